@@ -1,0 +1,240 @@
+/* milc_ks_gb300.h -- C ABI of the GB300-native improved-staggered hot path.
+ *
+ * One process drives one GPU.  Every entry point returns an int status
+ * (MKS_OK = 0, negative on error; mks_error_string() describes it) unless
+ * it is documented otherwise.  Arrays are plain C arrays in MILC's own
+ * memory layout for MILC_PRECISION=2, so a MILC build can pass its fields
+ * through unchanged:
+ *
+ *   colour vector field   double[V][6]       su3_vector[i]      (3 complex)
+ *   link field            double[V][4][18]   su3_matrix[4*i+dir] (3x3 complex, row major)
+ *   momentum field        double[V][4][10]   anti_hermitmat mom[dir] (m01,m02,m12,
+ *                                              m00im,m11im,m22im,space)
+ *
+ * where i is MILC's single-node site index: lexicographic
+ * x + nx*(y + ny*(z + nz*t)), even sites first (generic/layout_hyper_prime.c:
+ * 509-520).  Link fields carry the staggered phases and the antiperiodic
+ * time boundary folded in (generic_ks/rephase.c:99-117), as MILC's fermion
+ * links do.
+ *
+ * Operator conventions are MILC's (generic_ks/dslash_fn.c:365-576,
+ * generic_ks/mat_invert.c:18-44): D is anti-Hermitian without a factor 1/2,
+ *   (D s)(x) = sum_mu F_mu(x) s(x+mu) - F_mu(x-mu)^dag s(x-mu)
+ *            +       L_mu(x) s(x+3mu) - L_mu(x-3mu)^dag s(x-3mu),
+ * M = 2m + D, and the parity solves work with M^dag M = 4m^2 - D_eo D_oe.
+ *
+ * Host arrays stay owned by the caller; the library never frees them.
+ * Functions named *_dev take device pointers with the same layout and do
+ * no host<->device copies of field data.
+ */
+#ifndef MILC_KS_GB300_H
+#define MILC_KS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define MKS_OK              0
+#define MKS_ERR_ARG        -1   /* bad argument (size, parity, null pointer) */
+#define MKS_ERR_CUDA       -2   /* a CUDA runtime call failed */
+#define MKS_ERR_NOMEM      -3   /* device allocation failed */
+#define MKS_ERR_STATE      -4   /* library not initialised / lattice or links not loaded */
+#define MKS_ERR_TIMEOUT    -5   /* a bounded device-side wait gave up */
+#define MKS_ERR_NUMERIC    -6   /* NaN/Inf met in a solver recurrence */
+#define MKS_ERR_UNSUPPORTED -7  /* option not provided by this build */
+
+/* ---- parities: same values as MILC include/macros.h:17-19 ---- */
+#define MKS_ODD        0x01
+#define MKS_EVEN       0x02
+#define MKS_EVENANDODD 0x03
+
+/* ---- arithmetic precisions of the inner (sloppy) solve ----
+   MILC's qic->prec uses 1 = single, 2 = double (include/generic_quark_types.h:168) */
+#define MKS_PREC_HALF   0
+#define MKS_PREC_SINGLE 1
+#define MKS_PREC_DOUBLE 2
+
+/* Solver controls: the fields of MILC's quark_invert_control
+   (include/generic_quark_types.h:167-190) that the hot path reads. */
+typedef struct {
+  int    max;        /* iterations per restart (qic->max) */
+  int    nrestart;   /* maximum restarts (qic->nrestart); cap = max*nrestart */
+  int    parity;     /* MKS_EVEN, MKS_ODD (MKS_EVENANDODD where noted) */
+  int    prec;       /* inner precision: MKS_PREC_DOUBLE (plain FP64 CG),
+                        MKS_PREC_SINGLE or MKS_PREC_HALF (FP64 reliable updates) */
+  double resid;      /* target |r|/|b|, NOT squared (qic->resid) */
+  double relresid;   /* target Fermilab relative residual, 0 = unused (qic->relresid) */
+  double delta;      /* reliable-update trigger for mixed precision (0 -> 0.1) */
+} mks_invert_arg;
+
+/* Solver results: the fields MILC fills on return
+   (generic_ks/d_congrad5_fn_milc.c:370-395). */
+typedef struct {
+  double final_rsq;      /* true |r|^2/|b|^2 (squared, normalised) */
+  double final_relrsq;   /* relative residual, squared */
+  double size_r;         /* iterated residual, same normalisation */
+  double size_relr;
+  int    final_iters;
+  int    final_restart;
+  int    converged;      /* 1 converged, 0 not */
+  int    reliable_updates; /* FP64 true-residual recomputations (mixed precision) */
+} mks_invert_result;
+
+/* ------------------------------------------------------------------ */
+/* Library lifetime.  Replaces the QUDA set-up MILC performs in
+   initialize_quda() (generic/milc_to_quda_utilities.c:11-41). */
+int mks_init(int device);
+int mks_finalize(void);
+const char *mks_error_string(int status);
+/* Lattice extents (all even).  Frees every cached field of another size. */
+int mks_set_lattice(const int dims[4]);
+
+/* ------------------------------------------------------------------ */
+/* Fermion links.
+ * Replaces load_fatlinks_gpu / load_fatlonglinks_gpu
+ * (generic_ks/fermion_links_fn_load_gpu.c:19,49) and the QUDA link cache
+ * keyed on fn_links_t (include/fn_links.h:9-17, fresh_fn_links /
+ * cancel_quda_notification, generic_ks/d_congrad5_fn_gpu.c:121-126):
+ * fat and long links of one Naik-epsilon group are uploaded once into
+ * slot `slot` (0 .. MKS_MAX_SLOTS-1) and stay resident until reloaded or
+ * invalidated.  eps_naik is stored with the slot (fn->eps_naik). */
+#define MKS_MAX_SLOTS 12
+int mks_load_fn_links(int slot, const double *fat, const double *lng, double eps_naik);
+int mks_load_fn_links_dev(int slot, const double *fat_dev, const double *lng_dev, double eps_naik);
+int mks_invalidate_fn_links(int slot);
+int mks_get_fn_links(int slot, double *fat, double *lng);
+
+/* ------------------------------------------------------------------ */
+/* D_eo / D_oe.  Replaces dslash_fn_field (generic_ks/dslash_fn.c:302-358,
+ * generic_ks/dslash_fn_dblstore.c:285): dst on `parity` sites receives
+ * D src, src read on the other parity.  parity may be MKS_EVENANDODD. */
+int mks_dslash_fn_field(const double *src, double *dst, int parity, int slot);
+int mks_dslash_fn_field_dev(const double *src_dev, double *dst_dev, int parity, int slot);
+
+/* ------------------------------------------------------------------ */
+/* Single-source CG on (4m^2 - D_eo D_oe) for one parity.
+ * Replaces ks_congrad_parity_gpu (include/imp_ferm_links.h:95-97,
+ * generic_ks/d_congrad5_fn_gpu.c:35-165; CPU semantics
+ * generic_ks/d_congrad5_fn_milc.c:61-407).  dst holds the initial guess on
+ * entry and the solution on return; sites of the other parity are not
+ * touched.  A zero source gives a zero solution and 0 iterations.
+ * Returns the number of iterations (>= 0) or a negative status. */
+int mks_ks_congrad_parity(const double *src, double *dst, double mass, int slot,
+                          const mks_invert_arg *arg, mks_invert_result *res);
+int mks_ks_congrad_parity_dev(const double *src_dev, double *dst_dev, double mass, int slot,
+                              const mks_invert_arg *arg, mks_invert_result *res);
+
+/* Multi-source CG: nsrc right-hand sides solved together, every link read
+ * once per operator application for all sources.  Replaces
+ * ks_congrad_block_parity_gpu (include/imp_ferm_links.h:99-101,
+ * generic_ks/d_congrad5_fn_gpu.c:167-305).  res has nsrc entries.
+ * Returns the largest iteration count or a negative status. */
+int mks_ks_congrad_block_parity(int nsrc, const double *const *src, double *const *dst,
+                                double mass, int slot, const mks_invert_arg *arg,
+                                mks_invert_result *res);
+int mks_ks_congrad_block_parity_dev(int nsrc, const double *const *src_dev, double *const *dst_dev,
+                                    double mass, int slot, const mks_invert_arg *arg,
+                                    mks_invert_result *res);
+
+/* M^{-1} on both parities: precondition with M^dag, even CG, odd
+ * reconstruction, odd polish (generic_ks/mat_invert.c:328-407).  dst
+ * holds the initial guess.  arg->parity is ignored. */
+int mks_mat_invert_uml_field(const double *src, double *dst, double mass, int slot,
+                             const mks_invert_arg *arg, mks_invert_result *res);
+/* Same for nsrc sources (generic_ks/mat_invert.c:409-483); res[nsrc]. */
+int mks_mat_invert_block_uml(int nsrc, const double *const *src, double *const *dst,
+                             double mass, int slot, const mks_invert_arg *arg,
+                             mks_invert_result *res);
+
+/* Multi-shift CG: psim[j] = (sigma_j - D_eo D_oe)^{-1} src on arg->parity
+ * for offsets sigma_j > 0 (MILC's ksp[j].offset, sigma = 4 m^2 for a
+ * plain mass).  Replaces ks_multicg_offset_field_gpu
+ * (include/imp_ferm_links.h:211-218, generic_ks/ks_multicg_offset_gpu.c:
+ * 38-250; CPU semantics generic_ks/ks_multicg_offset.c:63-505).  Stops
+ * when the smallest shift meets arg->resid, like the CPU code (:381).
+ * psim is overwritten (zero initial guess).  res has num_offsets entries.
+ * arg->prec selects FP64, or FP32/FP16 shifted updates followed by an FP64
+ * refinement of every shift (generic_ks/ks_multicg.c:170-228). */
+int mks_ks_multicg_offset_field(const double *src, double *const *psim,
+                                const double *offsets, int num_offsets, int slot,
+                                const mks_invert_arg *arg, mks_invert_result *res);
+int mks_ks_multicg_offset_field_dev(const double *src_dev, double *const *psim_dev,
+                                    const double *offsets, int num_offsets, int slot,
+                                    const mks_invert_arg *arg, mks_invert_result *res);
+
+/* ------------------------------------------------------------------ */
+/* HISQ link construction.  Replaces load_hisq_aux_links_gpu and the fat /
+ * long smearing of load_hisq_fn_links (generic_ks/fermion_links_fn_load_gpu.c:
+ * 80-110, generic_ks/fermion_links_hisq_load_milc.c:547-640): from thin
+ * links U (phases in) build V = fat7(U), W = U(3) projection of V
+ * (analytic, generic_ks/su3_mat_op.c:828), and for each Naik group i the fat
+ * and long links X_i = asqtad+2xLepage(W) + eps_i (1-link + Naik)(W),
+ * stored in slots 0..n_naiks-1.  The aux links stay resident for the force.
+ * action: MKS_ACTION_HISQ; MKS_ACTION_ASQTAD builds asqtad fat/long links
+ * directly from U into slot 0 (tadpole factor u0). */
+#define MKS_ACTION_HISQ   1
+#define MKS_ACTION_ASQTAD 2
+int mks_load_links_from_thin(int action, const double *thin, int n_naiks,
+                             const double *eps_naik, double u0);
+int mks_get_hisq_aux(double *V, double *W);
+
+/* ------------------------------------------------------------------ */
+/* HISQ fermion force.  Replaces eo_fermion_force_multi with the GPU
+ * wrapper fn_fermion_force_multi_hisq_wrapper_mx_gpu
+ * (generic_ks/fermion_force_hisq_multi.c:155-219,2168-2290; CPU semantics
+ * :1182-1475): mom[dir](x) += TA( +-2 eps U_mu(x) dS/dU_mu(x) ) for the
+ * rational-function terms sum_j residues[j] |xxx_j><xxx_j| with xxx_j = X_j
+ * on even sites and D_oe X_j on odd sites.  n_orders_naik[g] gives how many
+ * consecutive terms belong to Naik group g (the first group counts every
+ * term).  Uses the aux links of the last mks_load_links_from_thin. */
+int mks_fermion_force_multi_hisq(double eps, const double *residues,
+                                 const double *const *xxx, int nterms,
+                                 const int *n_orders_naik, int n_naiks, double *mom);
+
+/* ------------------------------------------------------------------ */
+/* Kernel timing.  When enabled, the library brackets every launch of its
+ * kernels with CUDA events on its own stream; totals are per kernel family. */
+#define MKS_K_DSLASH_F64   0
+#define MKS_K_DSLASH_F32   1
+#define MKS_K_DSLASH_F16   2
+#define MKS_K_DSLASH_MRHS  3
+#define MKS_K_BLAS         4
+#define MKS_K_SHIFT        5
+#define MKS_K_LINKS        6
+#define MKS_K_FORCE        7
+#define MKS_K_COUNT        8
+int mks_timing_enable(int on);
+int mks_timing_reset(void);
+int mks_timing_get(int family, double *total_ms, long long *launches);
+/* Total kernel launches issued by the library since the last reset
+   (counted whether or not timing is enabled). */
+long long mks_launch_count(void);
+/* The library's CUDA stream, as a cudaStream_t cast to void*. */
+void *mks_stream(void);
+
+/* Run the D_eo kernel `iters` times at the given precision on resident
+ * copies of the slot's links and a resident random source, timing each
+ * launch with CUDA events (optionally writing a 256 MB buffer between
+ * launches to flush L2).  Returns the mean launch time in ms in *ms.
+ * nsrc > 1 times the multi-source kernel. */
+int mks_bench_dslash(int prec, int nsrc, int parity, int slot, int iters, int flush_l2,
+                     double *ms);
+
+/* ------------------------------------------------------------------ */
+/* Host-side synthetic inputs (no device work).  See mks_fields.c. */
+void   mks_site_coords(const int dims[4], size_t index, int xyzt[4]);
+size_t mks_site_index(const int dims[4], const int xyzt[4]);
+double mks_staggered_phase(const int dims[4], const int xyzt[4], int dir);
+int mks_gen_thin_links(const int dims[4], uint64_t seed, double a, double *links);
+int mks_apply_phases(const int dims[4], double *links, int sign);
+int mks_gen_vector(const int dims[4], uint64_t seed, int parity, double *vec);
+int mks_gen_momenta(const int dims[4], uint64_t seed, double *mom);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MILC_KS_GB300_H */
