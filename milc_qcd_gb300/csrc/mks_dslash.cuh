@@ -1,0 +1,175 @@
+// mks_dslash.cuh -- the improved-staggered D_eo kernel template.
+//
+// out(x) = sum_mu F_mu(x) in(x+mu) - F_mu(x-mu)^dag in(x-mu)
+//                + L_mu(x) in(x+3mu) - L_mu(x-3mu)^dag in(x-3mu)
+// (generic_ks/dslash_fn.c:365-576), for x of parity out_par.
+//
+// One thread group of G threads handles one output site; each thread of
+// the group applies the site's 16 links to NB sources, so a link fetched
+// from HBM serves G*NB right-hand sides (the G copies of a link load
+// within a warp coalesce into one request).  Neighbour indices are
+// computed from the checkerboard index; nothing but links and vectors is
+// read.  Epilogues fuse the CG / multi-shift BLAS and their dot products:
+//   EPI_PLAIN : out = D in
+//   EPI_AXPY  : out = D in + coef_s * p_s, with sums <p,out>, <out,r>, <out,out>
+//               (NSUM = 3, FEWSUMS-style CG) or only <p,out> (NSUM = 1)
+// followed by a grid reduction whose last block runs the finisher.
+#pragma once
+#include "mks_internal.cuh"
+#include "mks_reduce.cuh"
+
+namespace mks {
+
+constexpr int MAXSRC = 16;
+enum { EPI_PLAIN = 0, EPI_AXPY = 1 };
+
+template <class InT, class OutT, class EpiT>
+struct DslashArgs {
+  Geom g;
+  int out_par;
+  int nsrc;
+  int groups;                 // G (power of two, <= 8)
+  InT in[MAXSRC];
+  OutT out[MAXSRC];
+  EpiT p[MAXSRC];             // epilogue operand (same parity as out)
+  EpiT r[MAXSRC];
+  double coef[MAXSRC];
+  const int *skip;            // kernel returns at once when *skip != 0
+  const int *src_done;        // per-source: skip the epilogue update when non-zero
+  double *partials;
+  unsigned int *count;
+  double *totals;             // [nsrc][NSUM] written by the last block
+};
+
+template <typename R> struct EpiLoad;
+template <> struct EpiLoad<double> { typedef VecF64 type; };
+template <> struct EpiLoad<float> { typedef VecF32 type; };
+
+struct NoFinish {
+  __device__ void operator()(const double *, int) const {}
+};
+
+template <typename R, class LinkT, class InT, class OutT, int NB, int EPI, int NSUM, class Fin>
+__global__ void __launch_bounds__(256)
+k_dslash(const LinkT fat, const LinkT lng, const DslashArgs<InT, OutT, typename EpiLoad<R>::type> a,
+         const Fin fin) {
+  typedef typename EpiLoad<R>::type EpiT;
+  if (a.skip && *a.skip) return;
+  const Geom &g = a.g;
+  const int G = a.groups;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int h = tid / G, grp = tid - h * G;
+  const int Vh = g.Vh;
+  const int par = a.out_par, opar = 1 - par;
+  double sums[NB][NSUM > 0 ? NSUM : 1];
+#pragma unroll
+  for (int s = 0; s < NB; s++)
+#pragma unroll
+    for (int k = 0; k < (NSUM > 0 ? NSUM : 1); k++) sums[s][k] = 0.0;
+
+  if (h < Vh) {
+    int x, y, z, t;
+    site_coords(g, par, h, x, y, z, t);
+    V3<R> acc[NB];
+#pragma unroll
+    for (int s = 0; s < NB; s++)
+#pragma unroll
+      for (int c = 0; c < 3; c++) acc[s].c[c] = {R(0), R(0)};
+    const int c0[4] = {x, y, z, t};
+    const int L[4] = {g.nx, g.ny, g.nz, g.nt};
+#pragma unroll
+    for (int mu = 0; mu < 4; mu++) {
+      int cf1[4] = {c0[0], c0[1], c0[2], c0[3]}, cb1[4] = {c0[0], c0[1], c0[2], c0[3]};
+      int cf3[4] = {c0[0], c0[1], c0[2], c0[3]}, cb3[4] = {c0[0], c0[1], c0[2], c0[3]};
+      cf1[mu] = wrap_add(c0[mu], 1, L[mu]);
+      cb1[mu] = wrap_add(c0[mu], -1, L[mu]);
+      cf3[mu] = wrap_add(c0[mu], 3, L[mu]);
+      cb3[mu] = wrap_add(c0[mu], -3, L[mu]);
+      const int hf1 = cb_index(g, cf1[0], cf1[1], cf1[2], cf1[3]);
+      const int hb1 = cb_index(g, cb1[0], cb1[1], cb1[2], cb1[3]);
+      const int hf3 = cb_index(g, cf3[0], cf3[1], cf3[2], cf3[3]);
+      const int hb3 = cb_index(g, cb3[0], cb3[1], cb3[2], cb3[3]);
+      {
+        const M3<R> U = fat.load(par, mu, h, Vh);
+#pragma unroll
+        for (int s = 0; s < NB; s++) {
+          const int S = grp * NB + s;
+          if (S < a.nsrc) mv_acc(U, a.in[S].load(hf1, Vh), acc[s]);
+        }
+      }
+      {
+        const M3<R> U = lng.load(par, mu, h, Vh);
+#pragma unroll
+        for (int s = 0; s < NB; s++) {
+          const int S = grp * NB + s;
+          if (S < a.nsrc) mv_acc(U, a.in[S].load(hf3, Vh), acc[s]);
+        }
+      }
+      {
+        const M3<R> U = fat.load(opar, mu, hb1, Vh);
+#pragma unroll
+        for (int s = 0; s < NB; s++) {
+          const int S = grp * NB + s;
+          if (S < a.nsrc) amv_sub(U, a.in[S].load(hb1, Vh), acc[s]);
+        }
+      }
+      {
+        const M3<R> U = lng.load(opar, mu, hb3, Vh);
+#pragma unroll
+        for (int s = 0; s < NB; s++) {
+          const int S = grp * NB + s;
+          if (S < a.nsrc) amv_sub(U, a.in[S].load(hb3, Vh), acc[s]);
+        }
+      }
+    }
+#pragma unroll
+    for (int s = 0; s < NB; s++) {
+      const int S = grp * NB + s;
+      if (S >= a.nsrc) continue;
+      if (EPI == EPI_AXPY) {
+        const V3<R> p = a.p[S].load(h, Vh);
+        const R cf = (R)a.coef[S];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          acc[s].c[c].re = fma(cf, p.c[c].re, acc[s].c[c].re);
+          acc[s].c[c].im = fma(cf, p.c[c].im, acc[s].c[c].im);
+        }
+        if (NSUM >= 1) {
+          double d = 0;
+#pragma unroll
+          for (int c = 0; c < 3; c++) d += (double)p.c[c].re * acc[s].c[c].re + (double)p.c[c].im * acc[s].c[c].im;
+          sums[s][0] = d;
+        }
+        if (NSUM >= 3) {
+          const V3<R> r = a.r[S].load(h, Vh);
+          double d1 = 0, d2 = 0;
+#pragma unroll
+          for (int c = 0; c < 3; c++) {
+            d1 += (double)acc[s].c[c].re * r.c[c].re + (double)acc[s].c[c].im * r.c[c].im;
+            d2 += (double)acc[s].c[c].re * acc[s].c[c].re + (double)acc[s].c[c].im * acc[s].c[c].im;
+          }
+          sums[s][1] = d1;
+          sums[s][2] = d2;
+        }
+      }
+      a.out[S].store(h, Vh, acc[s]);
+    }
+  }
+  if (NSUM > 0) {
+    __shared__ double smem[(256 / 32 + 1) * MAXSRC * 3];
+    __shared__ double tot[MAXSRC * 3];
+    __shared__ double scratch[32];
+    block_reduce_grouped<NB, (NSUM > 0 ? NSUM : 1)>(sums, G, smem);
+    const int nslots = G * NB;
+    const double *btot = smem + (blockDim.x >> 5) * nslots * NSUM;
+    if (grid_reduce_last(btot, nslots * NSUM, a.partials, a.count, tot, scratch)) {
+      if (threadIdx.x == 0) {
+        for (int i = 0; i < a.nsrc * NSUM; i++) a.totals[i] = tot[i];
+      }
+      __syncthreads();
+      fin(tot, a.nsrc);
+    }
+  }
+}
+
+}  // namespace mks

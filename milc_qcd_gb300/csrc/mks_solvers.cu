@@ -1,0 +1,1517 @@
+// mks_solvers.cu -- D_eo launchers and the Krylov solvers behind the C ABI:
+//   mks_dslash_fn_field*          (generic_ks/dslash_fn.c:302-358)
+//   mks_ks_congrad_parity*        (generic_ks/d_congrad5_fn_milc.c:61-407,
+//                                  generic_ks/d_congrad5_fn_gpu.c:35-165)
+//   mks_ks_congrad_block_parity*  (generic_ks/d_congrad5_fn_gpu.c:167-305)
+//   mks_mat_invert_uml_field / mks_mat_invert_block_uml (generic_ks/mat_invert.c:328-483)
+//   mks_ks_multicg_offset_field*  (generic_ks/ks_multicg_offset.c:63-505,
+//                                  generic_ks/ks_multicg.c:170-228)
+//
+// Every iteration is device resident: the two D applications carry the
+// CG axpy and dot products in their epilogue, the solver scalars are
+// updated by the last block of each reduction, and kernels return at once
+// while a device flag asks for host attention (restart, reliable update,
+// convergence).  The host only polls that flag every few iterations.
+#include <cmath>
+#include <cstring>
+#include <cstdlib>
+#include <map>
+#include <string>
+#include <vector>
+#include "mks_internal.cuh"
+#include "mks_dslash.cuh"
+#include "mks_blas.cuh"
+
+namespace mks {
+
+// ------------------------------------------------------------------
+// workspace: named device buffers kept across calls
+struct WsBuf { void *p = nullptr; size_t bytes = 0; };
+static std::map<std::string, WsBuf> g_ws;
+
+static int ws(const std::string &name, size_t bytes, void **out) {
+  WsBuf &b = g_ws[name];
+  if (b.bytes < bytes) {
+    dev_free(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    MKS_TRY(dev_alloc(&b.p, bytes));
+    b.bytes = bytes;
+  }
+  *out = b.p;
+  return MKS_OK;
+}
+
+void ws_free_all() {
+  for (auto &kv : g_ws) dev_free(kv.second.p);
+  g_ws.clear();
+}
+
+template <typename T> static int wsv(const std::string &name, size_t n, T **out) {
+  void *p;
+  MKS_TRY(ws(name, n * sizeof(T), &p));
+  *out = (T *)p;
+  return MKS_OK;
+}
+
+// ------------------------------------------------------------------
+// solver scalars, one per source
+enum { ST_RUN = 0, ST_HOST = 1, ST_DONE = 4 };
+
+struct CgState {
+  double rsq;          // MILC 'rsq' (FEWSUMS estimate between true residuals)
+  double actual_rsq;   // true |r|^2 of the iterated residual
+  double a, b;
+  double source_norm;
+  double rsqmin, relrsqmin;
+  double size_r, size_relr;
+  double final_rsq, final_relrsq;
+  double maxrr, delta;
+  int iter, niter, max_cg, status;
+  int nrestart, max_restarts, mixed, converged;
+  int reliable;
+};
+
+struct Solver {
+  CgState *st = nullptr;   // device [nsrc]
+  int *skip = nullptr;     // device: non-zero while any source needs the host
+};
+
+// ---------- finishers ----------
+// after the second D of an iteration: pkp, c_tr, c_tt -> a, rsq, b
+// (generic_ks/d_congrad5_fn_milc.c:278-357 with FEWSUMS)
+struct FinCgAlpha {
+  CgState *st;
+  __device__ void operator()(const double *t, int nsrc) const {
+    int s = threadIdx.x;
+    if (s >= nsrc) return;
+    CgState &c = st[s];
+    if (c.status != ST_RUN) { c.a = 0; c.b = 0; return; }
+    double pkp = t[3 * s], c_tr = t[3 * s + 1], c_tt = t[3 * s + 2];
+    double oldrsq = c.actual_rsq;
+    double a = -c.rsq / pkp;
+    c.iter++;
+    c.a = a;
+    c.rsq = oldrsq + 2.0 * a * c_tr + a * a * c_tt;
+    c.b = c.rsq / oldrsq;
+    if (!isfinite(c.rsq) || !isfinite(a)) c.status = ST_HOST;
+  }
+};
+
+// after the update: true |r|^2 -> stop / restart / reliable-update checks.
+// FP64 CG: restart when iter % niter == 0 or the iterated residual meets
+// the target (d_congrad5_fn_milc.c:173-181).  Mixed precision: ask for a
+// reliable update when |r| fell below delta * max|r| since the last one,
+// or the iterated residual meets the target, or the iteration cap is hit.
+struct FinCgUpdate {
+  CgState *st;
+  int *skip;
+  __device__ void operator()(const double *t, int nsrc) const {
+    int s = threadIdx.x;
+    if (s < nsrc) {
+      CgState &c = st[s];
+      if (c.status == ST_RUN) {
+        c.actual_rsq = t[s];
+        c.size_r = c.rsq / c.source_norm;
+        if (c.mixed) {
+          double rn = sqrt(c.actual_rsq);
+          if (rn > c.maxrr) c.maxrr = rn;
+          if (rn < c.delta * c.maxrr || c.actual_rsq < c.rsqmin * c.source_norm || c.iter >= c.max_cg ||
+              !isfinite(c.actual_rsq))
+            c.status = ST_HOST;
+        } else {
+          if ((c.iter % c.niter == 0) || (c.rsqmin <= 0 || c.rsqmin > c.size_r) || !isfinite(c.actual_rsq))
+            c.status = ST_HOST;
+        }
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int any = 0;
+      for (int i = 0; i < nsrc; i++) any |= (st[i].status == ST_HOST);
+      *skip = any;
+    }
+  }
+};
+
+// source norm, and generic "store totals" finisher
+struct FinNone {
+  __device__ void operator()(const double *, int) const {}
+};
+
+// ---------- BLAS site operations ----------
+template <typename T> struct VT;
+template <> struct VT<double> { typedef double2 v2; };
+template <> struct VT<float> { typedef float2 v2; };
+
+struct PtrSet64 { double2 *p[BLAS_MAXSRC]; };
+struct PtrSet32 { float2 *p[BLAS_MAXSRC]; };
+struct PtrSet16 { __half2 *p[BLAS_MAXSRC]; float *n[BLAS_MAXSRC]; };
+
+// |v|^2
+template <typename T2> struct OpNorm {
+  T2 *v[BLAS_MAXSRC];
+  int Vh;
+  __device__ void operator()(int h, int s, double *out) const {
+    double a = 0;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      T2 q = v[s][(size_t)c * Vh + h];
+      a += (double)q.x * q.x + (double)q.y * q.y;
+    }
+    out[0] = a;
+  }
+};
+
+// CG restart / reliable update residual (FP64):
+//   ttt <- ttt - 4m^2 x ; r <- src + ttt ; sum |r|^2, and the relative residual
+//   sum |r|^2/|x|^2 (d_congrad5_fn_milc.c:196-216).  Optionally p <- r.
+struct OpResid64 {
+  double2 *ttt[BLAS_MAXSRC], *x[BLAS_MAXSRC], *src[BLAS_MAXSRC], *r[BLAS_MAXSRC], *p[BLAS_MAXSRC];
+  const CgState *st;
+  double msq4[BLAS_MAXSRC];
+  int Vh, setp;
+  __device__ void operator()(int h, int s, double *out) const {
+    if (st && st[s].status != ST_HOST) { out[0] = 0; out[1] = 0; return; }
+    double a = 0, xx = 0;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      size_t i = (size_t)c * Vh + h;
+      double2 t = ttt[s][i], xv = x[s][i], sv = src[s][i];
+      double2 rv = make_double2(sv.x + (t.x + (-msq4[s]) * xv.x), sv.y + (t.y + (-msq4[s]) * xv.y));
+      r[s][i] = rv;
+      if (setp) p[s][i] = rv;
+      a += rv.x * rv.x + rv.y * rv.y;
+      xx += xv.x * xv.x + xv.y * xv.y;
+    }
+    out[0] = a;
+    out[1] = (xx == 0) ? 1.0 : a / xx;
+  }
+};
+
+struct FinResid {
+  CgState *st;
+  int *skip;
+  __device__ void operator()(const double *t, int nsrc) const {
+    int s = threadIdx.x;
+    if (s < nsrc) {
+      CgState &c = st[s];
+      if (c.status == ST_HOST) {
+        c.rsq = t[2 * s];
+        c.actual_rsq = t[2 * s];
+        c.final_rsq = c.rsq / c.source_norm;
+        c.maxrr = sqrt(c.rsq);
+        c.iter++;
+      }
+    }
+  }
+};
+
+// CG update, FP64 or FP32 storage: x += a p; r += a ttt; sum |r|^2 (+ rel);
+// p = r + b p (d_congrad5_fn_milc.c:315-368).  Optional FP16 shadow of p.
+template <typename R> struct OpUpdate {
+  typedef typename VT<R>::v2 T2;
+  T2 *x[BLAS_MAXSRC], *p[BLAS_MAXSRC], *r[BLAS_MAXSRC], *ttt[BLAS_MAXSRC];
+  __half2 *p16[BLAS_MAXSRC];
+  float *p16n[BLAS_MAXSRC];
+  const CgState *st;
+  int Vh, relres;
+  __device__ void operator()(int h, int s, double *out) const {
+    const CgState &c = st[s];
+    if (c.status != ST_RUN) { out[0] = 0; if (relres) out[1] = 0; return; }
+    const R a = (R)c.a, b = (R)c.b;
+    double rr = 0, xx = 0;
+    V3<R> pn;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      size_t i = (size_t)k * Vh + h;
+      T2 xv = x[s][i], pv = p[s][i], rv = r[s][i], tv = ttt[s][i];
+      xv.x = xv.x + a * pv.x; xv.y = xv.y + a * pv.y;
+      rv.x = rv.x + a * tv.x; rv.y = rv.y + a * tv.y;
+      rr += (double)rv.x * rv.x + (double)rv.y * rv.y;
+      xx += (double)xv.x * xv.x + (double)xv.y * xv.y;
+      pv.x = rv.x + b * pv.x; pv.y = rv.y + b * pv.y;
+      x[s][i] = xv; r[s][i] = rv; p[s][i] = pv;
+      pn.c[k] = {(R)pv.x, (R)pv.y};
+    }
+    if (p16[s]) {
+      float m = 0.f;
+#pragma unroll
+      for (int k = 0; k < 3; k++) m = fmaxf(m, fmaxf(fabsf((float)pn.c[k].re), fabsf((float)pn.c[k].im)));
+      float inv = m > 0.f ? 1.f / m : 0.f;
+      p16n[s][h] = m;
+#pragma unroll
+      for (int k = 0; k < 3; k++)
+        p16[s][(size_t)k * Vh + h] = __floats2half2_rn((float)pn.c[k].re * inv, (float)pn.c[k].im * inv);
+    }
+    out[0] = rr;
+    if (relres) out[1] = (xx == 0) ? 1.0 : rr / xx;
+  }
+};
+
+// x64 += x32 ; x32 = 0 (reliable update), for flagged sources
+struct OpAccumX {
+  double2 *x64[BLAS_MAXSRC];
+  float2 *x32[BLAS_MAXSRC];
+  const CgState *st;
+  int Vh;
+  __device__ void operator()(int h, int s, double *) const {
+    if (st[s].status != ST_HOST) return;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      size_t i = (size_t)k * Vh + h;
+      double2 a = x64[s][i];
+      float2 b = x32[s][i];
+      x64[s][i] = make_double2(a.x + (double)b.x, a.y + (double)b.y);
+      x32[s][i] = make_float2(0.f, 0.f);
+    }
+  }
+};
+
+// r32 = r64, and (when setp) p32 = r32, p16 = r32, for flagged sources
+struct OpDemote {
+  double2 *r64[BLAS_MAXSRC];
+  float2 *r32[BLAS_MAXSRC], *p32[BLAS_MAXSRC];
+  __half2 *p16[BLAS_MAXSRC];
+  float *p16n[BLAS_MAXSRC];
+  const CgState *st;
+  int Vh, setp;
+  __device__ void operator()(int h, int s, double *) const {
+    if (st[s].status != ST_HOST) return;
+    float2 v[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      size_t i = (size_t)k * Vh + h;
+      double2 a = r64[s][i];
+      v[k] = make_float2((float)a.x, (float)a.y);
+      r32[s][i] = v[k];
+      if (setp) p32[s][i] = v[k];
+    }
+    if (setp && p16[s]) {
+      float m = 0.f;
+#pragma unroll
+      for (int k = 0; k < 3; k++) m = fmaxf(m, fmaxf(fabsf(v[k].x), fabsf(v[k].y)));
+      float inv = m > 0.f ? 1.f / m : 0.f;
+      p16n[s][h] = m;
+#pragma unroll
+      for (int k = 0; k < 3; k++) p16[s][(size_t)k * Vh + h] = __floats2half2_rn(v[k].x * inv, v[k].y * inv);
+    }
+  }
+};
+
+// zero a vector (one parity)
+template <typename T2> struct OpZero {
+  T2 *v[BLAS_MAXSRC];
+  int Vh;
+  __device__ void operator()(int h, int s, double *) const {
+#pragma unroll
+    for (int k = 0; k < 3; k++) { T2 z; z.x = 0; z.y = 0; v[s][(size_t)k * Vh + h] = z; }
+  }
+};
+
+template <class Op, int NSUM, class Fin>
+static int launch_site(int family, const Op &op, const Fin &fin, const int *skip, int nsrc, double *totals = nullptr) {
+  Context &c = ctx();
+  int Vh = (int)c.Vh;
+  int gx = grid_for(Vh, 256);
+  int cap = c.sm_count * 4;
+  if (gx > cap) gx = cap;
+  MKS_TRY(ensure_red(NSUM > 0 ? NSUM * nsrc : 1, gx));
+  timing_begin(family);
+  k_site<Op, NSUM, Fin><<<dim3(gx, nsrc), 256, 0, c.stream>>>(op, fin, skip, Vh, c.red.partials, c.red.count + 1,
+                                                             totals);
+  timing_end(family);
+  MKS_CUDA(cudaGetLastError());
+  return MKS_OK;
+}
+
+// ------------------------------------------------------------------
+// D_eo launchers
+struct LinkSet64 { LinkF64 fat, lng; };
+struct LinkSet32 { LinkF32 fat, lng; };
+struct LinkSet16 { LinkF16 fat, lng; };
+
+static LinkSet64 links64(const LinkSlot &s) { return {{s.fat64}, {s.lng64}}; }
+static LinkSet32 links32(const LinkSlot &s) { return {{s.fat32a, s.fat32b}, {s.lng32a, s.lng32b}}; }
+static LinkSet16 links16(const LinkSlot &s) {
+  return {{s.fat16a, s.fat16b, s.fat16scale}, {s.lng16a, s.lng16b, s.lng16scale}};
+}
+
+// thread-group shape for nsrc sources: G threads per site, NB sources each
+struct Shape { int G, NB; };
+static Shape shape_for(int nsrc) {
+  if (nsrc <= 1) return {1, 1};
+  if (nsrc <= 2) return {1, 2};
+  if (nsrc <= 4) return {1, 4};
+  if (nsrc <= 8) return {2, 4};
+  return {4, 4};
+}
+
+template <typename R, class LinkT, class InT, class OutT, int NB, int EPI, int NSUM, class Fin>
+static int launch_dslash_nb(int family, const LinkT &fat, const LinkT &lng,
+                            DslashArgs<InT, OutT, typename EpiLoad<R>::type> &a, const Fin &fin) {
+  Context &c = ctx();
+  size_t threads = (size_t)c.Vh * a.groups;
+  int block = 256;
+  int grid = (int)((threads + block - 1) / block);
+  if (NSUM > 0) {
+    MKS_TRY(ensure_red(NSUM * a.groups * NB, grid));
+    a.partials = c.red.partials;
+    a.count = c.red.count;
+  }
+  timing_begin(family);
+  k_dslash<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin><<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
+  timing_end(family);
+  MKS_CUDA(cudaGetLastError());
+  return MKS_OK;
+}
+
+template <typename R, class LinkT, class InT, class OutT, int EPI, int NSUM, class Fin>
+static int launch_dslash(int family, const LinkT &fat, const LinkT &lng,
+                         DslashArgs<InT, OutT, typename EpiLoad<R>::type> &a, const Fin &fin) {
+  Shape sh = shape_for(a.nsrc);
+  a.groups = sh.G;
+  a.g = ctx().geom;
+  if (a.nsrc > 1 && family != MKS_K_DSLASH_F64) family = MKS_K_DSLASH_MRHS;
+  switch (sh.NB) {
+  case 1: return launch_dslash_nb<R, LinkT, InT, OutT, 1, EPI, NSUM, Fin>(family, fat, lng, a, fin);
+  case 2: return launch_dslash_nb<R, LinkT, InT, OutT, 2, EPI, NSUM, Fin>(family, fat, lng, a, fin);
+  default: return launch_dslash_nb<R, LinkT, InT, OutT, 4, EPI, NSUM, Fin>(family, fat, lng, a, fin);
+  }
+}
+
+// plain D on FP64 SoA fields, nsrc sources
+static int dslash64(const LinkSlot &sl, int out_par, int nsrc, double2 *const *in, double2 *const *out,
+                    const int *skip = nullptr) {
+  DslashArgs<VecF64, VecF64, VecF64> a;
+  memset(&a, 0, sizeof a);
+  a.out_par = out_par; a.nsrc = nsrc; a.skip = skip;
+  for (int s = 0; s < nsrc; s++) { a.in[s].p = in[s]; a.out[s].p = out[s]; }
+  LinkSet64 L = links64(sl);
+  return launch_dslash<double, LinkF64, VecF64, VecF64, EPI_PLAIN, 0>(MKS_K_DSLASH_F64, L.fat, L.lng, a, FinNone());
+}
+
+// ------------------------------------------------------------------
+// per-parity field views inside one contiguous "full" SoA buffer:
+// full field = [2][3][Vh] double2; parity par starts at par*3*Vh
+static inline double2 *par64(double2 *full, int par) { return full + (size_t)par * 3 * ctx().Vh; }
+
+static int parity_index(int parity, int *par) {
+  if (parity == MKS_EVEN) *par = 0;
+  else if (parity == MKS_ODD) *par = 1;
+  else return MKS_ERR_ARG;
+  return MKS_OK;
+}
+
+static int slot_ok(int slot) {
+  if (slot < 0 || slot >= MKS_MAX_SLOTS) return MKS_ERR_ARG;
+  if (!ctx().slots[slot].valid) return MKS_ERR_STATE;
+  return MKS_OK;
+}
+
+// ------------------------------------------------------------------
+// public D
+static int dslash_dev_impl(const double *src_dev, double *dst_dev, int parity, int slot) {
+  Context &c = ctx();
+  double2 *in, *out;
+  MKS_TRY(wsv("ds_in", 6 * c.Vh, &in));
+  MKS_TRY(wsv("ds_out", 6 * c.Vh, &out));
+  const LinkSlot &sl = c.slots[slot];
+  for (int op = 0; op < 2; op++) {
+    int out_par = op;
+    bool want = (parity == MKS_EVENANDODD) || (parity == MKS_EVEN && op == 0) || (parity == MKS_ODD && op == 1);
+    if (!want) continue;
+    MKS_TRY(vec_aos_to_soa64(src_dev, par64(in, 1 - out_par), 1 - out_par));
+  }
+  for (int op = 0; op < 2; op++) {
+    bool want = (parity == MKS_EVENANDODD) || (parity == MKS_EVEN && op == 0) || (parity == MKS_ODD && op == 1);
+    if (!want) continue;
+    double2 *pin = par64(in, 1 - op), *pout = par64(out, op);
+    MKS_TRY(dslash64(sl, op, 1, &pin, &pout));
+    MKS_TRY(vec_soa64_to_aos(pout, dst_dev, op));
+  }
+  return MKS_OK;
+}
+
+}  // namespace mks
+
+using namespace mks;
+
+extern "C" int mks_dslash_fn_field_dev(const double *src_dev, double *dst_dev, int parity, int slot) {
+  MKS_TRY(check_ready());
+  MKS_TRY(slot_ok(slot));
+  if (!src_dev || !dst_dev || parity < MKS_ODD || parity > MKS_EVENANDODD) return MKS_ERR_ARG;
+  MKS_TRY(dslash_dev_impl(src_dev, dst_dev, parity, slot));
+  MKS_CUDA(cudaStreamSynchronize(ctx().stream));
+  return MKS_OK;
+}
+
+extern "C" int mks_dslash_fn_field(const double *src, double *dst, int parity, int slot) {
+  MKS_TRY(check_ready());
+  MKS_TRY(slot_ok(slot));
+  if (!src || !dst || parity < MKS_ODD || parity > MKS_EVENANDODD) return MKS_ERR_ARG;
+  Context &c = ctx();
+  size_t bytes = c.V * 6 * sizeof(double);
+  double *ds, *dd;
+  MKS_TRY(wsv("host_src", 6 * c.V, &ds));
+  MKS_TRY(wsv("host_dst", 6 * c.V, &dd));
+  MKS_CUDA(cudaMemcpyAsync(ds, src, bytes, cudaMemcpyHostToDevice, c.stream));
+  MKS_CUDA(cudaMemcpyAsync(dd, dst, bytes, cudaMemcpyHostToDevice, c.stream));
+  MKS_TRY(dslash_dev_impl(ds, dd, parity, slot));
+  MKS_CUDA(cudaMemcpyAsync(dst, dd, bytes, cudaMemcpyDeviceToHost, c.stream));
+  MKS_CUDA(cudaStreamSynchronize(c.stream));
+  return MKS_OK;
+}
+
+namespace mks {
+
+// ------------------------------------------------------------------
+// block CG driver (nsrc = 1 is the single-source solver)
+struct CgFields {
+  // FP64, one parity [3][Vh] per source
+  double2 *src[MAXSRC], *x[MAXSRC], *r[MAXSRC], *p[MAXSRC], *ttt[MAXSRC], *t[MAXSRC];  // t: other parity
+  // sloppy
+  float2 *x32[MAXSRC], *r32[MAXSRC], *p32[MAXSRC], *ttt32[MAXSRC], *t32[MAXSRC];
+  __half2 *p16[MAXSRC], *t16[MAXSRC];
+  float *p16n[MAXSRC], *t16n[MAXSRC];
+};
+
+static int alloc_cg_fields(CgFields &f, int nsrc, int prec) {
+  Context &c = ctx();
+  size_t n = 3 * c.Vh;
+  for (int s = 0; s < nsrc; s++) {
+    std::string k = std::to_string(s);
+    MKS_TRY(wsv("cg_src" + k, n, &f.src[s]));
+    MKS_TRY(wsv("cg_x" + k, n, &f.x[s]));
+    MKS_TRY(wsv("cg_r" + k, n, &f.r[s]));
+    MKS_TRY(wsv("cg_p" + k, n, &f.p[s]));
+    MKS_TRY(wsv("cg_ttt" + k, n, &f.ttt[s]));
+    MKS_TRY(wsv("cg_t" + k, n, &f.t[s]));
+    if (prec != MKS_PREC_DOUBLE) {
+      MKS_TRY(wsv("cg_x32" + k, n, &f.x32[s]));
+      MKS_TRY(wsv("cg_r32" + k, n, &f.r32[s]));
+      MKS_TRY(wsv("cg_p32" + k, n, &f.p32[s]));
+      MKS_TRY(wsv("cg_ttt32" + k, n, &f.ttt32[s]));
+      MKS_TRY(wsv("cg_t32" + k, n, &f.t32[s]));
+      if (prec == MKS_PREC_HALF) {
+        MKS_TRY(wsv("cg_p16" + k, n, &f.p16[s]));
+        MKS_TRY(wsv("cg_t16" + k, n, &f.t16[s]));
+        MKS_TRY(wsv("cg_p16n" + k, c.Vh, &f.p16n[s]));
+        MKS_TRY(wsv("cg_t16n" + k, c.Vh, &f.t16n[s]));
+      } else {
+        f.p16[s] = nullptr; f.t16[s] = nullptr; f.p16n[s] = nullptr; f.t16n[s] = nullptr;
+      }
+    }
+  }
+  return MKS_OK;
+}
+
+// ttt <- D_par D_opar x  (FP64) for the sources listed
+static int apply_DD64(const LinkSlot &sl, int par, int nsrc, double2 *const *x, double2 *const *t,
+                      double2 *const *ttt) {
+  MKS_TRY(dslash64(sl, 1 - par, nsrc, x, t));
+  MKS_TRY(dslash64(sl, par, nsrc, t, ttt));
+  return MKS_OK;
+}
+
+static int read_states(Solver &S, int nsrc, CgState *h) {
+  Context &c = ctx();
+  MKS_CUDA(cudaMemcpyAsync(h, S.st, nsrc * sizeof(CgState), cudaMemcpyDeviceToHost, c.stream));
+  MKS_CUDA(cudaStreamSynchronize(c.stream));
+  return MKS_OK;
+}
+static int write_states(Solver &S, int nsrc, const CgState *h, int skip) {
+  Context &c = ctx();
+  MKS_CUDA(cudaMemcpyAsync(S.st, h, nsrc * sizeof(CgState), cudaMemcpyHostToDevice, c.stream));
+  MKS_CUDA(cudaMemcpyAsync(S.skip, &skip, sizeof(int), cudaMemcpyHostToDevice, c.stream));
+  MKS_CUDA(cudaStreamSynchronize(c.stream));
+  return MKS_OK;
+}
+
+// one sloppy or FP64 CG iteration for all running sources (3 launches)
+static int cg_iteration(const LinkSlot &sl, int par, int nsrc, int prec, const double *msq4, CgFields &f, Solver &S) {
+  if (prec == MKS_PREC_DOUBLE) {
+    DslashArgs<VecF64, VecF64, VecF64> a1;
+    memset(&a1, 0, sizeof a1);
+    a1.out_par = 1 - par; a1.nsrc = nsrc; a1.skip = S.skip;
+    for (int s = 0; s < nsrc; s++) { a1.in[s].p = f.p[s]; a1.out[s].p = f.t[s]; }
+    LinkSet64 L = links64(sl);
+    MKS_TRY((launch_dslash<double, LinkF64, VecF64, VecF64, EPI_PLAIN, 0>(MKS_K_DSLASH_F64, L.fat, L.lng, a1, FinNone())));
+    DslashArgs<VecF64, VecF64, VecF64> a2;
+    memset(&a2, 0, sizeof a2);
+    a2.out_par = par; a2.nsrc = nsrc; a2.skip = S.skip;
+    for (int s = 0; s < nsrc; s++) {
+      a2.in[s].p = f.t[s]; a2.out[s].p = f.ttt[s]; a2.p[s].p = f.p[s]; a2.r[s].p = f.r[s]; a2.coef[s] = -msq4[s];
+    }
+    double *tot;
+    MKS_TRY(wsv("cg_tot", 3 * MAXSRC, &tot));
+    a2.totals = tot;
+    MKS_TRY((launch_dslash<double, LinkF64, VecF64, VecF64, EPI_AXPY, 3>(MKS_K_DSLASH_F64, L.fat, L.lng, a2, FinCgAlpha{S.st})));
+    OpUpdate<double> up;
+    memset(&up, 0, sizeof up);
+    for (int s = 0; s < nsrc; s++) { up.x[s] = f.x[s]; up.p[s] = f.p[s]; up.r[s] = f.r[s]; up.ttt[s] = f.ttt[s]; }
+    up.st = S.st; up.Vh = (int)ctx().Vh; up.relres = 0;
+    MKS_TRY((launch_site<OpUpdate<double>, 1, FinCgUpdate>(MKS_K_BLAS, up, FinCgUpdate{S.st, S.skip}, S.skip, nsrc)));
+    return MKS_OK;
+  }
+  const int fam = prec == MKS_PREC_SINGLE ? MKS_K_DSLASH_F32 : MKS_K_DSLASH_F16;
+  if (prec == MKS_PREC_SINGLE) {
+    LinkSet32 L = links32(sl);
+    DslashArgs<VecF32, VecF32, VecF32> a1;
+    memset(&a1, 0, sizeof a1);
+    a1.out_par = 1 - par; a1.nsrc = nsrc; a1.skip = S.skip;
+    for (int s = 0; s < nsrc; s++) { a1.in[s].p = f.p32[s]; a1.out[s].p = f.t32[s]; }
+    MKS_TRY((launch_dslash<float, LinkF32, VecF32, VecF32, EPI_PLAIN, 0>(fam, L.fat, L.lng, a1, FinNone())));
+    DslashArgs<VecF32, VecF32, VecF32> a2;
+    memset(&a2, 0, sizeof a2);
+    a2.out_par = par; a2.nsrc = nsrc; a2.skip = S.skip;
+    for (int s = 0; s < nsrc; s++) {
+      a2.in[s].p = f.t32[s]; a2.out[s].p = f.ttt32[s]; a2.p[s].p = f.p32[s]; a2.r[s].p = f.r32[s]; a2.coef[s] = -msq4[s];
+    }
+    double *tot;
+    MKS_TRY(wsv("cg_tot", 3 * MAXSRC, &tot));
+    a2.totals = tot;
+    MKS_TRY((launch_dslash<float, LinkF32, VecF32, VecF32, EPI_AXPY, 3>(fam, L.fat, L.lng, a2, FinCgAlpha{S.st})));
+  } else {
+    LinkSet16 L = links16(sl);
+    DslashArgs<VecF16, VecF16, VecF32> a1;
+    memset(&a1, 0, sizeof a1);
+    a1.out_par = 1 - par; a1.nsrc = nsrc; a1.skip = S.skip;
+    for (int s = 0; s < nsrc; s++) {
+      a1.in[s].p = f.p16[s]; a1.in[s].norm = f.p16n[s]; a1.out[s].p = f.t16[s]; a1.out[s].norm = f.t16n[s];
+    }
+    MKS_TRY((launch_dslash<float, LinkF16, VecF16, VecF16, EPI_PLAIN, 0>(fam, L.fat, L.lng, a1, FinNone())));
+    DslashArgs<VecF16, VecF32, VecF32> a2;
+    memset(&a2, 0, sizeof a2);
+    a2.out_par = par; a2.nsrc = nsrc; a2.skip = S.skip;
+    for (int s = 0; s < nsrc; s++) {
+      a2.in[s].p = f.t16[s]; a2.in[s].norm = f.t16n[s]; a2.out[s].p = f.ttt32[s];
+      a2.p[s].p = f.p32[s]; a2.r[s].p = f.r32[s]; a2.coef[s] = -msq4[s];
+    }
+    double *tot;
+    MKS_TRY(wsv("cg_tot", 3 * MAXSRC, &tot));
+    a2.totals = tot;
+    MKS_TRY((launch_dslash<float, LinkF16, VecF16, VecF32, EPI_AXPY, 3>(fam, L.fat, L.lng, a2, FinCgAlpha{S.st})));
+  }
+  OpUpdate<float> up;
+  memset(&up, 0, sizeof up);
+  for (int s = 0; s < nsrc; s++) {
+    up.x[s] = f.x32[s]; up.p[s] = f.p32[s]; up.r[s] = f.r32[s]; up.ttt[s] = f.ttt32[s];
+    up.p16[s] = f.p16[s]; up.p16n[s] = f.p16n[s];
+  }
+  up.st = S.st; up.Vh = (int)ctx().Vh; up.relres = 0;
+  MKS_TRY((launch_site<OpUpdate<float>, 1, FinCgUpdate>(MKS_K_BLAS, up, FinCgUpdate{S.st, S.skip}, S.skip, nsrc)));
+  return MKS_OK;
+}
+
+// FP64 true residual for sources with status ST_HOST: r = src - M^dag M x,
+// |r|^2 -> state (rsq, actual_rsq, final_rsq, iter++).  setp: p <- r.
+static int true_residual(const LinkSlot &sl, int par, int nsrc, const double *msq4, CgFields &f, Solver &S, int setp,
+                         std::vector<double> *relrsq) {
+  MKS_TRY(apply_DD64(sl, par, nsrc, f.x, f.t, f.ttt));
+  OpResid64 op;
+  memset(&op, 0, sizeof op);
+  for (int s = 0; s < nsrc; s++) { op.ttt[s] = f.ttt[s]; op.x[s] = f.x[s]; op.src[s] = f.src[s]; op.r[s] = f.r[s]; op.p[s] = f.p[s]; }
+  op.st = S.st; for (int s = 0; s < nsrc; s++) op.msq4[s] = msq4[s]; op.Vh = (int)ctx().Vh; op.setp = setp;
+  double *tot;
+  MKS_TRY(wsv("cg_tot2", 2 * MAXSRC, &tot));
+  MKS_TRY((launch_site<OpResid64, 2, FinResid>(MKS_K_BLAS, op, FinResid{S.st, S.skip}, nullptr, nsrc, tot)));
+  if (relrsq) {
+    std::vector<double> h(2 * nsrc);
+    Context &c = ctx();
+    MKS_CUDA(cudaMemcpyAsync(h.data(), tot, 2 * nsrc * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    MKS_CUDA(cudaStreamSynchronize(c.stream));
+    relrsq->resize(nsrc);
+    for (int s = 0; s < nsrc; s++) (*relrsq)[s] = sqrt(2.0 * h[2 * s + 1] / (double)c.V);
+  }
+  return MKS_OK;
+}
+
+static int poll_interval() {
+  static int v = -1;
+  if (v < 0) {
+    const char *e = getenv("MKS_POLL");
+    v = e ? atoi(e) : 8;
+    if (v < 1) v = 1;
+  }
+  return v;
+}
+
+// Solve (sigma_s - D_par D_opar) x_s = src_s on parity par for nsrc sources
+// held in FP64 SoA device fields f.src/f.x (x = initial guess on entry);
+// sigma_s = 4 m^2 for a plain mass, or a multi-shift offset when refining.
+static int block_cg_shifted(int slot, int par, int nsrc, const double *msq4, const mks_invert_arg *arg,
+                            CgFields &f, mks_invert_result *res) {
+  Context &c = ctx();
+  const LinkSlot &sl = c.slots[slot];
+  const int prec = arg->prec;
+  const bool mixed = prec != MKS_PREC_DOUBLE;
+  Solver S;
+  MKS_TRY(wsv("cg_state", MAXSRC, &S.st));
+  MKS_TRY(wsv("cg_skip", 1, &S.skip));
+
+  // source norms
+  {
+    OpNorm<double2> op;
+    memset(&op, 0, sizeof op);
+    for (int s = 0; s < nsrc; s++) op.v[s] = f.src[s];
+    op.Vh = (int)c.Vh;
+    double *tot;
+    MKS_TRY(wsv("cg_tot1", MAXSRC, &tot));
+    MKS_TRY((launch_site<OpNorm<double2>, 1, FinNone>(MKS_K_BLAS, op, FinNone(), nullptr, nsrc, tot)));
+    std::vector<double> h(nsrc);
+    MKS_CUDA(cudaMemcpyAsync(h.data(), tot, nsrc * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    MKS_CUDA(cudaStreamSynchronize(c.stream));
+    std::vector<CgState> hs(nsrc);
+    memset(hs.data(), 0, nsrc * sizeof(CgState));
+    for (int s = 0; s < nsrc; s++) {
+      CgState &q = hs[s];
+      q.source_norm = h[s];
+      q.rsqmin = arg->resid * arg->resid;
+      q.relrsqmin = arg->relresid * arg->relresid;
+      q.niter = arg->max > 0 ? arg->max : 1;
+      q.max_restarts = arg->nrestart > 0 ? arg->nrestart : 1;
+      q.max_cg = q.niter * q.max_restarts;
+      q.mixed = mixed;
+      q.delta = arg->delta > 0 ? arg->delta : 0.1;
+      q.size_relr = 1.0;
+      q.converged = 1;
+      q.status = ST_HOST;
+      if (h[s] == 0.0) q.status = ST_DONE;  // trivial source: zero solution
+    }
+    MKS_TRY(write_states(S, nsrc, hs.data(), 1));
+    for (int s = 0; s < nsrc; s++)
+      if (h[s] == 0.0) MKS_CUDA(cudaMemsetAsync(f.x[s], 0, 3 * c.Vh * sizeof(double2), c.stream));
+  }
+  if (mixed) {
+    OpZero<float2> z;
+    for (int s = 0; s < nsrc; s++) z.v[s] = f.x32[s];
+    z.Vh = (int)c.Vh;
+    MKS_TRY((launch_site<OpZero<float2>, 0, FinNone>(MKS_K_BLAS, z, FinNone(), nullptr, nsrc)));
+  }
+  std::vector<CgState> hs(nsrc);
+  bool first = true;
+  int guard = 0;
+  while (true) {
+    MKS_TRY(read_states(S, nsrc, hs.data()));
+    bool any_host = false, any_run = false;
+    for (int s = 0; s < nsrc; s++) {
+      any_host |= hs[s].status == ST_HOST;
+      any_run |= hs[s].status == ST_RUN;
+    }
+    if (any_host) {
+      // restart (FP64 CG) or reliable update (mixed): recompute the true residual
+      if (mixed && !first) {
+        OpAccumX ax;
+        memset(&ax, 0, sizeof ax);
+        for (int s = 0; s < nsrc; s++) { ax.x64[s] = f.x[s]; ax.x32[s] = f.x32[s]; }
+        ax.st = S.st; ax.Vh = (int)c.Vh;
+        MKS_TRY((launch_site<OpAccumX, 0, FinNone>(MKS_K_BLAS, ax, FinNone(), nullptr, nsrc)));
+      }
+      std::vector<double> relrsq;
+      MKS_TRY(true_residual(sl, par, nsrc, msq4, f, S, mixed ? (first ? 1 : 0) : 1,
+                            arg->relresid > 0 ? &relrsq : nullptr));
+      if (mixed) {
+        OpDemote dm;
+        memset(&dm, 0, sizeof dm);
+        for (int s = 0; s < nsrc; s++) {
+          dm.r64[s] = f.r[s]; dm.r32[s] = f.r32[s]; dm.p32[s] = f.p32[s]; dm.p16[s] = f.p16[s]; dm.p16n[s] = f.p16n[s];
+        }
+        dm.st = S.st; dm.Vh = (int)c.Vh; dm.setp = first ? 1 : 0;
+        MKS_TRY((launch_site<OpDemote, 0, FinNone>(MKS_K_BLAS, dm, FinNone(), nullptr, nsrc)));
+      }
+      MKS_TRY(read_states(S, nsrc, hs.data()));
+      for (int s = 0; s < nsrc; s++) {
+        CgState &q = hs[s];
+        if (q.status != ST_HOST) continue;
+        if (!relrsq.empty()) q.final_relrsq = relrsq[s] * relrsq[s];
+        bool ok = (q.rsqmin <= 0 || q.rsqmin > q.final_rsq) &&
+                  (q.relrsqmin <= 0 || q.relrsqmin > q.final_relrsq);
+        if (mixed) {
+          if (!first) q.reliable++;
+          if (ok || q.iter >= q.max_cg || !std::isfinite(q.final_rsq)) {
+            q.status = ST_DONE;
+            q.converged = ok ? 1 : 0;
+          } else {
+            q.status = ST_RUN;
+          }
+        } else {
+          // d_congrad5_fn_milc.c:229-241
+          if (q.iter >= q.max_cg || q.nrestart >= q.max_restarts || ok || !std::isfinite(q.final_rsq)) {
+            q.status = ST_DONE;
+            q.converged = (q.nrestart == q.max_restarts || q.iter >= q.max_cg || !ok) ? 0 : 1;
+          } else {
+            q.nrestart++;
+            q.status = ST_RUN;
+          }
+        }
+      }
+      first = false;
+      any_run = false;
+      for (int s = 0; s < nsrc; s++) any_run |= hs[s].status == ST_RUN;
+      MKS_TRY(write_states(S, nsrc, hs.data(), 0));
+    }
+    if (!any_run) break;
+    int np = poll_interval();
+    for (int k = 0; k < np; k++) MKS_TRY(cg_iteration(sl, par, nsrc, prec, msq4, f, S));
+    if (++guard > 10000000) return MKS_ERR_TIMEOUT;
+  }
+  if (mixed) {
+    // x64 already holds the accumulated solution: the last reliable update folded x32 in
+  }
+  for (int s = 0; s < nsrc; s++) {
+    CgState &q = hs[s];
+    mks_invert_result &o = res[s];
+    o.final_rsq = q.final_rsq;
+    o.final_relrsq = q.final_relrsq;
+    o.size_r = q.size_r;
+    o.size_relr = q.size_relr;
+    o.final_iters = q.iter;
+    o.final_restart = q.nrestart;
+    o.converged = q.converged;
+    o.reliable_updates = q.reliable;
+  }
+  return MKS_OK;
+}
+
+static int block_cg(int slot, int par, int nsrc, double mass, const mks_invert_arg *arg, CgFields &f,
+                    mks_invert_result *res) {
+  double msq4[MAXSRC];
+  for (int s = 0; s < nsrc; s++) msq4[s] = 4.0 * mass * mass;
+  return block_cg_shifted(slot, par, nsrc, msq4, arg, f, res);
+}
+
+static int check_arg(const mks_invert_arg *arg, bool need_parity) {
+  if (!arg) return MKS_ERR_ARG;
+  if (arg->prec != MKS_PREC_DOUBLE && arg->prec != MKS_PREC_SINGLE && arg->prec != MKS_PREC_HALF) return MKS_ERR_ARG;
+  if (need_parity && arg->parity != MKS_EVEN && arg->parity != MKS_ODD) return MKS_ERR_ARG;
+  if (arg->max <= 0 || arg->nrestart <= 0) return MKS_ERR_ARG;
+  return MKS_OK;
+}
+
+// dev variant core: fields already in device AoS FP64 (MILC layout)
+static int congrad_block_dev(int nsrc, const double *const *src_dev, double *const *dst_dev, double mass, int slot,
+                             const mks_invert_arg *arg, mks_invert_result *res) {
+  int par;
+  MKS_TRY(parity_index(arg->parity, &par));
+  CgFields f;
+  memset(&f, 0, sizeof f);
+  MKS_TRY(alloc_cg_fields(f, nsrc, arg->prec));
+  for (int s = 0; s < nsrc; s++) {
+    MKS_TRY(vec_aos_to_soa64(src_dev[s], f.src[s], par));
+    MKS_TRY(vec_aos_to_soa64(dst_dev[s], f.x[s], par));
+  }
+  MKS_TRY(block_cg(slot, par, nsrc, mass, arg, f, res));
+  for (int s = 0; s < nsrc; s++) MKS_TRY(vec_soa64_to_aos(f.x[s], dst_dev[s], par));
+  MKS_CUDA(cudaStreamSynchronize(ctx().stream));
+  return MKS_OK;
+}
+
+// host arrays: copy in, solve in batches of MAXSRC, copy out
+static int congrad_block_host(int nsrc, const double *const *src, double *const *dst, double mass, int slot,
+                              const mks_invert_arg *arg, mks_invert_result *res) {
+  Context &c = ctx();
+  size_t bytes = c.V * 6 * sizeof(double);
+  for (int b0 = 0; b0 < nsrc; b0 += MAXSRC) {
+    int nb = nsrc - b0 < MAXSRC ? nsrc - b0 : MAXSRC;
+    double *ds[MAXSRC], *dd[MAXSRC];
+    for (int s = 0; s < nb; s++) {
+      MKS_TRY(wsv("hsrc" + std::to_string(s), 6 * c.V, &ds[s]));
+      MKS_TRY(wsv("hdst" + std::to_string(s), 6 * c.V, &dd[s]));
+      MKS_CUDA(cudaMemcpyAsync(ds[s], src[b0 + s], bytes, cudaMemcpyHostToDevice, c.stream));
+      MKS_CUDA(cudaMemcpyAsync(dd[s], dst[b0 + s], bytes, cudaMemcpyHostToDevice, c.stream));
+    }
+    MKS_TRY(congrad_block_dev(nb, ds, dd, mass, slot, arg, res + b0));
+    for (int s = 0; s < nb; s++) MKS_CUDA(cudaMemcpyAsync(dst[b0 + s], dd[s], bytes, cudaMemcpyDeviceToHost, c.stream));
+    MKS_CUDA(cudaStreamSynchronize(c.stream));
+  }
+  return MKS_OK;
+}
+
+static int max_iters(int nsrc, const mks_invert_result *res) {
+  int m = 0;
+  for (int s = 0; s < nsrc; s++) m = res[s].final_iters > m ? res[s].final_iters : m;
+  return m;
+}
+
+}  // namespace mks
+
+extern "C" {
+
+int mks_ks_congrad_parity_dev(const double *src_dev, double *dst_dev, double mass, int slot,
+                              const mks_invert_arg *arg, mks_invert_result *res) {
+  MKS_TRY(check_ready());
+  MKS_TRY(slot_ok(slot));
+  MKS_TRY(check_arg(arg, true));
+  if (!src_dev || !dst_dev || !res) return MKS_ERR_ARG;
+  MKS_TRY(congrad_block_dev(1, &src_dev, &dst_dev, mass, slot, arg, res));
+  return res[0].final_iters;
+}
+
+int mks_ks_congrad_parity(const double *src, double *dst, double mass, int slot, const mks_invert_arg *arg,
+                          mks_invert_result *res) {
+  MKS_TRY(check_ready());
+  MKS_TRY(slot_ok(slot));
+  MKS_TRY(check_arg(arg, true));
+  if (!src || !dst || !res) return MKS_ERR_ARG;
+  MKS_TRY(congrad_block_host(1, &src, &dst, mass, slot, arg, res));
+  return res[0].final_iters;
+}
+
+int mks_ks_congrad_block_parity_dev(int nsrc, const double *const *src_dev, double *const *dst_dev, double mass,
+                                    int slot, const mks_invert_arg *arg, mks_invert_result *res) {
+  MKS_TRY(check_ready());
+  MKS_TRY(slot_ok(slot));
+  MKS_TRY(check_arg(arg, true));
+  if (nsrc <= 0 || nsrc > MAXSRC || !src_dev || !dst_dev || !res) return MKS_ERR_ARG;
+  MKS_TRY(congrad_block_dev(nsrc, src_dev, dst_dev, mass, slot, arg, res));
+  return max_iters(nsrc, res);
+}
+
+int mks_ks_congrad_block_parity(int nsrc, const double *const *src, double *const *dst, double mass, int slot,
+                                const mks_invert_arg *arg, mks_invert_result *res) {
+  MKS_TRY(check_ready());
+  MKS_TRY(slot_ok(slot));
+  MKS_TRY(check_arg(arg, true));
+  if (nsrc <= 0 || !src || !dst || !res) return MKS_ERR_ARG;
+  MKS_TRY(congrad_block_host(nsrc, src, dst, mass, slot, arg, res));
+  return max_iters(nsrc, res);
+}
+
+}  // extern "C"
+
+namespace mks {
+
+// out = alpha*a + beta*b (FP64, one parity, per source)
+struct OpLin64 {
+  double2 *out[BLAS_MAXSRC], *a[BLAS_MAXSRC], *b[BLAS_MAXSRC];
+  double alpha, beta;
+  int Vh;
+  __device__ void operator()(int h, int s, double *) const {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      size_t i = (size_t)k * Vh + h;
+      double2 x = a[s][i], y = b[s][i];
+      out[s][i] = make_double2(alpha * x.x + beta * y.x, alpha * x.y + beta * y.y);
+    }
+  }
+};
+
+static int lin64(int nsrc, double2 *const *out, double alpha, double2 *const *a, double beta, double2 *const *b) {
+  OpLin64 op;
+  memset(&op, 0, sizeof op);
+  for (int s = 0; s < nsrc; s++) { op.out[s] = out[s]; op.a[s] = a[s]; op.b[s] = b[s]; }
+  op.alpha = alpha; op.beta = beta; op.Vh = (int)ctx().Vh;
+  return launch_site<OpLin64, 0, FinNone>(MKS_K_BLAS, op, FinNone(), nullptr, nsrc);
+}
+
+// M^{-1} for nsrc sources given device AoS fields (generic_ks/mat_invert.c:328-483):
+//   tmp = M^dag src = 2m src - D src; even CG on tmp; dst_o = (src_o - D_oe dst_e)/(2m);
+//   odd CG on tmp (polish).
+static int mat_invert_dev(int nsrc, const double *const *src_dev, double *const *dst_dev, double mass, int slot,
+                          const mks_invert_arg *arg, mks_invert_result *res) {
+  Context &c = ctx();
+  const LinkSlot &sl = c.slots[slot];
+  CgFields f;
+  memset(&f, 0, sizeof f);
+  MKS_TRY(alloc_cg_fields(f, nsrc, arg->prec));
+  double2 *se[MAXSRC], *so[MAXSRC], *te[MAXSRC], *to[MAXSRC], *de[MAXSRC], *dn[MAXSRC];
+  size_t n = 3 * c.Vh;
+  for (int s = 0; s < nsrc; s++) {
+    std::string k = std::to_string(s);
+    MKS_TRY(wsv("mi_se" + k, n, &se[s])); MKS_TRY(wsv("mi_so" + k, n, &so[s]));
+    MKS_TRY(wsv("mi_te" + k, n, &te[s])); MKS_TRY(wsv("mi_to" + k, n, &to[s]));
+    MKS_TRY(wsv("mi_de" + k, n, &de[s])); MKS_TRY(wsv("mi_dn" + k, n, &dn[s]));
+    MKS_TRY(vec_aos_to_soa64(src_dev[s], se[s], 0));
+    MKS_TRY(vec_aos_to_soa64(src_dev[s], so[s], 1));
+    MKS_TRY(vec_aos_to_soa64(dst_dev[s], f.x[s], 0));
+  }
+  // tmp_e = 2m src_e - D src_o ; tmp_o = 2m src_o - D src_e
+  MKS_TRY(dslash64(sl, 0, nsrc, so, de));
+  MKS_TRY(dslash64(sl, 1, nsrc, se, dn));
+  MKS_TRY(lin64(nsrc, te, 2.0 * mass, se, -1.0, de));
+  MKS_TRY(lin64(nsrc, to, 2.0 * mass, so, -1.0, dn));
+  // even solve
+  mks_invert_arg a = *arg;
+  a.parity = MKS_EVEN;
+  for (int s = 0; s < nsrc; s++)
+    MKS_CUDA(cudaMemcpyAsync(f.src[s], te[s], n * sizeof(double2), cudaMemcpyDeviceToDevice, c.stream));
+  std::vector<mks_invert_result> r_even(nsrc);
+  MKS_TRY(block_cg(slot, 0, nsrc, mass, &a, f, r_even.data()));
+  // odd reconstruction: dst_o = (src_o - D_oe dst_e) / (2m)
+  for (int s = 0; s < nsrc; s++)
+    MKS_CUDA(cudaMemcpyAsync(de[s], f.x[s], n * sizeof(double2), cudaMemcpyDeviceToDevice, c.stream));
+  MKS_TRY(dslash64(sl, 1, nsrc, de, dn));
+  MKS_TRY(lin64(nsrc, f.x, 1.0 / (2.0 * mass), so, -1.0 / (2.0 * mass), dn));
+  // odd polish
+  a.parity = MKS_ODD;
+  for (int s = 0; s < nsrc; s++)
+    MKS_CUDA(cudaMemcpyAsync(f.src[s], to[s], n * sizeof(double2), cudaMemcpyDeviceToDevice, c.stream));
+  MKS_TRY(block_cg(slot, 1, nsrc, mass, &a, f, res));
+  for (int s = 0; s < nsrc; s++) {
+    res[s].final_iters += r_even[s].final_iters;
+    MKS_TRY(vec_soa64_to_aos(de[s], dst_dev[s], 0));
+    MKS_TRY(vec_soa64_to_aos(f.x[s], dst_dev[s], 1));
+  }
+  MKS_CUDA(cudaStreamSynchronize(c.stream));
+  return MKS_OK;
+}
+
+static int mat_invert_host(int nsrc, const double *const *src, double *const *dst, double mass, int slot,
+                           const mks_invert_arg *arg, mks_invert_result *res) {
+  Context &c = ctx();
+  size_t bytes = c.V * 6 * sizeof(double);
+  for (int b0 = 0; b0 < nsrc; b0 += MAXSRC) {
+    int nb = nsrc - b0 < MAXSRC ? nsrc - b0 : MAXSRC;
+    double *ds[MAXSRC], *dd[MAXSRC];
+    for (int s = 0; s < nb; s++) {
+      MKS_TRY(wsv("hsrc" + std::to_string(s), 6 * c.V, &ds[s]));
+      MKS_TRY(wsv("hdst" + std::to_string(s), 6 * c.V, &dd[s]));
+      MKS_CUDA(cudaMemcpyAsync(ds[s], src[b0 + s], bytes, cudaMemcpyHostToDevice, c.stream));
+      MKS_CUDA(cudaMemcpyAsync(dd[s], dst[b0 + s], bytes, cudaMemcpyHostToDevice, c.stream));
+    }
+    MKS_TRY(mat_invert_dev(nb, ds, dd, mass, slot, arg, res + b0));
+    for (int s = 0; s < nb; s++) MKS_CUDA(cudaMemcpyAsync(dst[b0 + s], dd[s], bytes, cudaMemcpyDeviceToHost, c.stream));
+    MKS_CUDA(cudaStreamSynchronize(c.stream));
+  }
+  return MKS_OK;
+}
+
+}  // namespace mks
+
+extern "C" {
+
+int mks_mat_invert_uml_field(const double *src, double *dst, double mass, int slot, const mks_invert_arg *arg,
+                             mks_invert_result *res) {
+  MKS_TRY(check_ready());
+  MKS_TRY(slot_ok(slot));
+  MKS_TRY(check_arg(arg, false));
+  if (!src || !dst || !res || mass == 0.0) return MKS_ERR_ARG;
+  MKS_TRY(mat_invert_host(1, &src, &dst, mass, slot, arg, res));
+  return res[0].final_iters;
+}
+
+int mks_mat_invert_block_uml(int nsrc, const double *const *src, double *const *dst, double mass, int slot,
+                             const mks_invert_arg *arg, mks_invert_result *res) {
+  MKS_TRY(check_ready());
+  MKS_TRY(slot_ok(slot));
+  MKS_TRY(check_arg(arg, false));
+  if (nsrc <= 0 || !src || !dst || !res || mass == 0.0) return MKS_ERR_ARG;
+  MKS_TRY(mat_invert_host(nsrc, src, dst, mass, slot, arg, res));
+  return max_iters(nsrc, res);
+}
+
+}  // extern "C"
+
+namespace mks {
+
+// deterministic pseudo-random fill for benchmark inputs
+__global__ void k_fill_bench(float2 *v, size_t n, unsigned seed) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    unsigned a = (unsigned)i * 2654435761u ^ seed, b = a * 1664525u + 1013904223u;
+    v[i] = make_float2((a >> 8) * (1.0f / 16777216.0f) - 0.5f, (b >> 8) * (1.0f / 16777216.0f) - 0.5f);
+  }
+}
+__global__ void k_f32_to_f64(const float2 *a, double2 *b, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    b[i] = make_double2(a[i].x, a[i].y);
+}
+__global__ void k_f32_to_f16(const float2 *a, __half2 *b, float *nrm, int Vh) {
+  int h = blockIdx.x * blockDim.x + threadIdx.x;
+  if (h >= Vh) return;
+  float m = 0.f;
+  for (int c = 0; c < 3; c++) m = fmaxf(m, fmaxf(fabsf(a[(size_t)c * Vh + h].x), fabsf(a[(size_t)c * Vh + h].y)));
+  float inv = m > 0 ? 1.f / m : 0.f;
+  nrm[h] = m;
+  for (int c = 0; c < 3; c++) b[(size_t)c * Vh + h] = __floats2half2_rn(a[(size_t)c * Vh + h].x * inv, a[(size_t)c * Vh + h].y * inv);
+}
+__global__ void k_flush(float4 *buf, size_t n, float v) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    buf[i] = make_float4(v, v, v, v);
+}
+
+}  // namespace mks
+
+extern "C" int mks_bench_dslash(int prec, int nsrc, int parity, int slot, int iters, int flush_l2, double *ms) {
+  MKS_TRY(check_ready());
+  MKS_TRY(slot_ok(slot));
+  if (nsrc < 1 || nsrc > MAXSRC || iters < 1 || !ms) return MKS_ERR_ARG;
+  int par;
+  MKS_TRY(parity_index(parity, &par));
+  Context &c = ctx();
+  const LinkSlot &sl = c.slots[slot];
+  size_t n = 3 * c.Vh;
+  float2 *in32[MAXSRC], *out32[MAXSRC];
+  double2 *in64[MAXSRC], *out64[MAXSRC];
+  __half2 *in16[MAXSRC];
+  float *in16n[MAXSRC];
+  for (int s = 0; s < nsrc; s++) {
+    std::string k = std::to_string(s);
+    MKS_TRY(wsv("bd_in32" + k, n, &in32[s]));
+    MKS_TRY(wsv("bd_out32" + k, n, &out32[s]));
+    k_fill_bench<<<c.sm_count * 4, 256, 0, c.stream>>>(in32[s], n, 1234u + s);
+    if (prec == MKS_PREC_DOUBLE) {
+      MKS_TRY(wsv("bd_in64" + k, n, &in64[s]));
+      MKS_TRY(wsv("bd_out64" + k, n, &out64[s]));
+      k_f32_to_f64<<<c.sm_count * 4, 256, 0, c.stream>>>(in32[s], in64[s], n);
+    } else if (prec == MKS_PREC_HALF) {
+      MKS_TRY(wsv("bd_in16" + k, n, &in16[s]));
+      MKS_TRY(wsv("bd_in16n" + k, c.Vh, &in16n[s]));
+      k_f32_to_f16<<<grid_for(c.Vh, 256), 256, 0, c.stream>>>(in32[s], in16[s], in16n[s], (int)c.Vh);
+    }
+  }
+  float4 *flush = nullptr;
+  size_t nflush = (size_t)256 << 20;  // bytes
+  if (flush_l2) MKS_TRY(wsv("bd_flush", nflush / sizeof(float4), &flush));
+  MKS_CUDA(cudaGetLastError());
+  cudaEvent_t e0, e1;
+  MKS_CUDA(cudaEventCreate(&e0));
+  MKS_CUDA(cudaEventCreate(&e1));
+  double total = 0;
+  for (int it = 0; it < iters + 1; it++) {  // first launch is a warm-up
+    if (flush) k_flush<<<c.sm_count * 4, 256, 0, c.stream>>>(flush, nflush / sizeof(float4), (float)it);
+    MKS_CUDA(cudaEventRecord(e0, c.stream));
+    if (prec == MKS_PREC_DOUBLE) {
+      MKS_TRY(dslash64(sl, par, nsrc, in64, out64));
+    } else if (prec == MKS_PREC_SINGLE) {
+      DslashArgs<VecF32, VecF32, VecF32> a;
+      memset(&a, 0, sizeof a);
+      a.out_par = par; a.nsrc = nsrc;
+      for (int s = 0; s < nsrc; s++) { a.in[s].p = in32[s]; a.out[s].p = out32[s]; }
+      LinkSet32 L = links32(sl);
+      MKS_TRY((launch_dslash<float, LinkF32, VecF32, VecF32, EPI_PLAIN, 0>(MKS_K_DSLASH_F32, L.fat, L.lng, a, FinNone())));
+    } else {
+      DslashArgs<VecF16, VecF32, VecF32> a;
+      memset(&a, 0, sizeof a);
+      a.out_par = par; a.nsrc = nsrc;
+      for (int s = 0; s < nsrc; s++) { a.in[s].p = in16[s]; a.in[s].norm = in16n[s]; a.out[s].p = out32[s]; }
+      LinkSet16 L = links16(sl);
+      MKS_TRY((launch_dslash<float, LinkF16, VecF16, VecF32, EPI_PLAIN, 0>(MKS_K_DSLASH_F16, L.fat, L.lng, a, FinNone())));
+    }
+    MKS_CUDA(cudaEventRecord(e1, c.stream));
+    MKS_CUDA(cudaEventSynchronize(e1));
+    float t = 0;
+    MKS_CUDA(cudaEventElapsedTime(&t, e0, e1));
+    if (it > 0) total += t;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms = total / iters;
+  return MKS_OK;
+}
+
+// ====================================================================
+// Multi-shift CG (generic_ks/ks_multicg_offset.c:63-505).
+// Per iteration: K1 t = D_oe p; K2 ttt = D_eo t + shift0 p with
+// pkp, <ttt,r>, |ttt|^2 and, in its last block, every shift's zeta/beta/
+// alpha recurrence; K3 one pass over all shifts: psim_j += beta_j pm_j,
+// r += beta ttt, pm_j = zeta_j r + alpha_j pm_j, p = pm_low, and the true
+// |r|^2 that decides convergence.  alpha uses |r_new|^2 expanded from the
+// K2 sums (the FEWSUMS device of d_congrad5_fn_milc.c:296-312), so the
+// shift updates need only the one pass.
+namespace mks {
+
+constexpr int MAXSH = 32;
+
+struct MsState {
+  double rsq, pkp, source_norm, rsqstop, shift0;
+  double shifts[MAXSH], zeta_i[MAXSH], zeta_im1[MAXSH], zeta_ip1[MAXSH];
+  double beta_i[MAXSH], beta_im1[MAXSH], alpha[MAXSH];
+  int iter, niter, status, j_low, num_now, num_offsets, need_scroll, pad;
+};
+
+struct FinMsAlpha {
+  MsState *st;
+  __device__ void operator()(const double *t, int) const {
+    if (threadIdx.x != 0) return;
+    MsState &m = *st;
+    if (m.status != ST_RUN) return;
+    if (m.need_scroll) {
+      for (int j = 0; j < m.num_now; j++) {
+        m.beta_im1[j] = m.beta_i[j];
+        m.zeta_im1[j] = m.zeta_i[j];
+        m.zeta_i[j] = m.zeta_ip1[j];
+      }
+      m.need_scroll = 0;
+    }
+    const int jl = m.j_low;
+    double pkp = t[0], c_tr = t[1], c_tt = t[2];
+    m.pkp = pkp;
+    m.iter++;
+    m.beta_i[jl] = -m.rsq / pkp;
+    m.zeta_ip1[jl] = 1.0;
+    for (int j = 0; j < m.num_now; j++) {
+      if (j == jl) continue;
+      m.zeta_ip1[j] = m.zeta_i[j] * m.zeta_im1[j] * m.beta_im1[jl];
+      double c1 = m.beta_i[jl] * m.alpha[jl] * (m.zeta_im1[j] - m.zeta_i[j]);
+      double c2 = m.zeta_im1[j] * m.beta_im1[jl] * (1.0 + m.shifts[j] * m.beta_i[jl]);
+      if (c1 + c2 != 0.0) m.zeta_ip1[j] /= c1 + c2;
+      else m.zeta_ip1[j] = 0.0;
+      if (m.zeta_i[j] != 0.0) {
+        m.beta_i[j] = m.beta_i[jl] * m.zeta_ip1[j] / m.zeta_i[j];
+      } else {
+        m.zeta_ip1[j] = 0.0;
+        m.beta_i[j] = 0.0;
+        if (j == m.num_now - 1 && j > jl) m.num_now--;
+      }
+    }
+    // |r + beta ttt|^2 from the K2 sums
+    double b = m.beta_i[jl];
+    double rsq_new = m.rsq + 2.0 * b * c_tr + b * b * c_tt;
+    m.alpha[jl] = rsq_new / m.rsq;
+    for (int j = 0; j < m.num_now; j++) {
+      if (j == jl) continue;
+      if (m.zeta_i[j] * m.beta_i[jl] != 0.0)
+        m.alpha[j] = m.alpha[jl] * m.zeta_ip1[j] * m.beta_i[j] / (m.zeta_i[j] * m.beta_i[jl]);
+      else
+        m.alpha[j] = 0.0;
+    }
+    if (!isfinite(m.beta_i[jl])) m.status = ST_HOST;
+  }
+};
+
+struct FinMsUpdate {
+  MsState *st;
+  int *skip;
+  __device__ void operator()(const double *t, int) const {
+    if (threadIdx.x != 0) return;
+    MsState &m = *st;
+    if (m.status == ST_RUN) {
+      m.rsq = t[0];
+      m.need_scroll = 1;
+      if ((m.rsqstop > 0 && m.rsq <= m.rsqstop) || m.iter >= m.niter || !isfinite(m.rsq)) m.status = ST_HOST;
+    }
+    *skip = (m.status != ST_RUN);
+  }
+};
+
+template <typename R> struct OpShiftUpdate {
+  typedef typename VT<R>::v2 T2;
+  T2 *psim[MAXSH], *pm[MAXSH];
+  T2 *r, *ttt, *cgp;
+  __half2 *p16;
+  float *p16n;
+  const MsState *st;
+  int Vh;
+  __device__ void operator()(int h, int, double *out) const {
+    const MsState &m = *st;
+    const int n = m.num_now, jl = m.j_low;
+    const R bl = (R)m.beta_i[jl];
+    T2 rn[3];
+    double rr = 0;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      size_t i = (size_t)k * Vh + h;
+      T2 rv = r[i], tv = ttt[i];
+      rv.x = rv.x + bl * tv.x; rv.y = rv.y + bl * tv.y;
+      rn[k] = rv;
+      r[i] = rv;
+      rr += (double)rv.x * rv.x + (double)rv.y * rv.y;
+    }
+    for (int j = 0; j < n; j++) {
+      const R bj = (R)m.beta_i[j], zj = (R)m.zeta_ip1[j], aj = (R)m.alpha[j];
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        size_t i = (size_t)k * Vh + h;
+        T2 pv = pm[j][i], xv = psim[j][i];
+        xv.x = xv.x + bj * pv.x; xv.y = xv.y + bj * pv.y;
+        pv.x = zj * rn[k].x + aj * pv.x; pv.y = zj * rn[k].y + aj * pv.y;
+        psim[j][i] = xv;
+        pm[j][i] = pv;
+        if (j == jl) cgp[i] = pv;
+      }
+      if (j == jl && p16) {
+        float mx = 0.f;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          T2 pv = pm[j][(size_t)k * Vh + h];
+          mx = fmaxf(mx, fmaxf(fabsf((float)pv.x), fabsf((float)pv.y)));
+        }
+        float inv = mx > 0.f ? 1.f / mx : 0.f;
+        p16n[h] = mx;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          T2 pv = pm[j][(size_t)k * Vh + h];
+          p16[(size_t)k * Vh + h] = __floats2half2_rn((float)pv.x * inv, (float)pv.y * inv);
+        }
+      }
+    }
+    out[0] = rr;
+  }
+};
+
+// initial fields: r = p = pm_j = src (converted), psim_j = 0
+template <typename R> struct OpShiftInit {
+  typedef typename VT<R>::v2 T2;
+  T2 *psim[MAXSH], *pm[MAXSH];
+  T2 *r, *cgp;
+  const double2 *src;
+  __half2 *p16;
+  float *p16n;
+  int Vh, n;
+  __device__ void operator()(int h, int, double *out) const {
+    double a = 0;
+    float mx = 0.f;
+    T2 v[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      size_t i = (size_t)k * Vh + h;
+      double2 sv = src[i];
+      v[k].x = (R)sv.x; v[k].y = (R)sv.y;
+      r[i] = v[k]; cgp[i] = v[k];
+      a += sv.x * sv.x + sv.y * sv.y;
+      mx = fmaxf(mx, fmaxf(fabsf((float)sv.x), fabsf((float)sv.y)));
+      for (int j = 0; j < n; j++) {
+        pm[j][i] = v[k];
+        T2 z; z.x = 0; z.y = 0;
+        psim[j][i] = z;
+      }
+    }
+    if (p16) {
+      float inv = mx > 0.f ? 1.f / mx : 0.f;
+      p16n[h] = mx;
+#pragma unroll
+      for (int k = 0; k < 3; k++) p16[(size_t)k * Vh + h] = __floats2half2_rn((float)v[k].x * inv, (float)v[k].y * inv);
+    }
+    out[0] = a;
+  }
+};
+
+struct OpF32ToF64 {
+  const float2 *a[BLAS_MAXSRC];
+  double2 *b[BLAS_MAXSRC];
+  int Vh;
+  __device__ void operator()(int h, int s, double *) const {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      size_t i = (size_t)k * Vh + h;
+      float2 v = a[s][i];
+      b[s][i] = make_double2(v.x, v.y);
+    }
+  }
+};
+
+// sloppy (or FP64) multi-shift iterations; R selects vector storage precision
+template <typename R>
+static int multishift_core(const LinkSlot &sl, int par, int prec, const double2 *src64, int nsh,
+                           const double *offsets, double resid, int niter, void **psim_out, MsState *hstate) {
+  typedef typename VT<R>::v2 T2;
+  Context &c = ctx();
+  const int Vh = (int)c.Vh;
+  size_t n = 3 * c.Vh;
+  T2 *r, *cgp, *ttt, *t, *pm[MAXSH], *psim[MAXSH];
+  const char *tag = sizeof(R) == 8 ? "64" : "32";
+  MKS_TRY(wsv(std::string("ms_r") + tag, n, &r));
+  MKS_TRY(wsv(std::string("ms_p") + tag, n, &cgp));
+  MKS_TRY(wsv(std::string("ms_ttt") + tag, n, &ttt));
+  MKS_TRY(wsv(std::string("ms_t") + tag, n, &t));
+  for (int j = 0; j < nsh; j++) {
+    MKS_TRY(wsv(std::string("ms_pm") + tag + "_" + std::to_string(j), n, &pm[j]));
+    MKS_TRY(wsv(std::string("ms_x") + tag + "_" + std::to_string(j), n, &psim[j]));
+    psim_out[j] = psim[j];
+  }
+  __half2 *p16 = nullptr, *t16 = nullptr;
+  float *p16n = nullptr, *t16n = nullptr;
+  if (prec == MKS_PREC_HALF) {
+    MKS_TRY(wsv("ms_p16", n, &p16)); MKS_TRY(wsv("ms_t16", n, &t16));
+    MKS_TRY(wsv("ms_p16n", c.Vh, &p16n)); MKS_TRY(wsv("ms_t16n", c.Vh, &t16n));
+  }
+  MsState *st;
+  int *skip;
+  MKS_TRY(wsv("ms_state", 1, &st));
+  MKS_TRY(wsv("ms_skip", 1, &skip));
+  // initial state (ks_multicg_offset.c:180-262)
+  MsState h;
+  memset(&h, 0, sizeof h);
+  double offset_low = 1.0e20;
+  int j_low = -1;
+  for (int j = 0; j < nsh; j++) {
+    h.shifts[j] = offsets[j];
+    if (offsets[j] < offset_low) { offset_low = offsets[j]; j_low = j; }
+  }
+  for (int j = 0; j < nsh; j++)
+    if (j != j_low) h.shifts[j] -= h.shifts[j_low];
+  h.shift0 = -h.shifts[j_low];
+  h.j_low = j_low; h.num_now = nsh; h.num_offsets = nsh; h.niter = niter;
+  for (int j = 0; j < nsh; j++) { h.zeta_im1[j] = h.zeta_i[j] = 1.0; h.beta_im1[j] = -1.0; h.alpha[j] = 0.0; }
+  {
+    OpShiftInit<R> op;
+    memset(&op, 0, sizeof op);
+    for (int j = 0; j < nsh; j++) { op.psim[j] = psim[j]; op.pm[j] = pm[j]; }
+    op.r = r; op.cgp = cgp; op.src = src64; op.p16 = p16; op.p16n = p16n; op.Vh = Vh; op.n = nsh;
+    double *tot;
+    MKS_TRY(wsv("ms_tot", 4, &tot));
+    MKS_TRY((launch_site<OpShiftInit<R>, 1, FinNone>(MKS_K_SHIFT, op, FinNone(), nullptr, 1, tot)));
+    double sn = 0;
+    MKS_CUDA(cudaMemcpyAsync(&sn, tot, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    MKS_CUDA(cudaStreamSynchronize(c.stream));
+    h.source_norm = sn;
+    h.rsq = sn;
+    h.rsqstop = resid * resid * sn;
+    h.iter = 1;
+    h.status = sn == 0.0 ? ST_DONE : ST_RUN;
+  }
+  MKS_CUDA(cudaMemcpyAsync(st, &h, sizeof h, cudaMemcpyHostToDevice, c.stream));
+  int zero = 0;
+  MKS_CUDA(cudaMemcpyAsync(skip, &zero, sizeof zero, cudaMemcpyHostToDevice, c.stream));
+  double *tot;
+  MKS_TRY(wsv("ms_tot3", 4, &tot));
+  int guard = 0;
+  while (h.status == ST_RUN) {
+    for (int k = 0; k < poll_interval(); k++) {
+      if (prec == MKS_PREC_DOUBLE) {
+        LinkSet64 L = links64(sl);
+        DslashArgs<VecF64, VecF64, VecF64> a1;
+        memset(&a1, 0, sizeof a1);
+        a1.out_par = 1 - par; a1.nsrc = 1; a1.skip = skip;
+        a1.in[0].p = (double2 *)cgp; a1.out[0].p = (double2 *)t;
+        MKS_TRY((launch_dslash<double, LinkF64, VecF64, VecF64, EPI_PLAIN, 0>(MKS_K_DSLASH_F64, L.fat, L.lng, a1, FinNone())));
+        DslashArgs<VecF64, VecF64, VecF64> a2;
+        memset(&a2, 0, sizeof a2);
+        a2.out_par = par; a2.nsrc = 1; a2.skip = skip; a2.totals = tot;
+        a2.in[0].p = (double2 *)t; a2.out[0].p = (double2 *)ttt; a2.p[0].p = (double2 *)cgp; a2.r[0].p = (double2 *)r;
+        a2.coef[0] = h.shift0;
+        MKS_TRY((launch_dslash<double, LinkF64, VecF64, VecF64, EPI_AXPY, 3>(MKS_K_DSLASH_F64, L.fat, L.lng, a2, FinMsAlpha{st})));
+      } else if (prec == MKS_PREC_SINGLE) {
+        LinkSet32 L = links32(sl);
+        DslashArgs<VecF32, VecF32, VecF32> a1;
+        memset(&a1, 0, sizeof a1);
+        a1.out_par = 1 - par; a1.nsrc = 1; a1.skip = skip;
+        a1.in[0].p = (float2 *)cgp; a1.out[0].p = (float2 *)t;
+        MKS_TRY((launch_dslash<float, LinkF32, VecF32, VecF32, EPI_PLAIN, 0>(MKS_K_DSLASH_F32, L.fat, L.lng, a1, FinNone())));
+        DslashArgs<VecF32, VecF32, VecF32> a2;
+        memset(&a2, 0, sizeof a2);
+        a2.out_par = par; a2.nsrc = 1; a2.skip = skip; a2.totals = tot;
+        a2.in[0].p = (float2 *)t; a2.out[0].p = (float2 *)ttt; a2.p[0].p = (float2 *)cgp; a2.r[0].p = (float2 *)r;
+        a2.coef[0] = h.shift0;
+        MKS_TRY((launch_dslash<float, LinkF32, VecF32, VecF32, EPI_AXPY, 3>(MKS_K_DSLASH_F32, L.fat, L.lng, a2, FinMsAlpha{st})));
+      } else {
+        LinkSet16 L = links16(sl);
+        DslashArgs<VecF16, VecF16, VecF32> a1;
+        memset(&a1, 0, sizeof a1);
+        a1.out_par = 1 - par; a1.nsrc = 1; a1.skip = skip;
+        a1.in[0].p = p16; a1.in[0].norm = p16n; a1.out[0].p = t16; a1.out[0].norm = t16n;
+        MKS_TRY((launch_dslash<float, LinkF16, VecF16, VecF16, EPI_PLAIN, 0>(MKS_K_DSLASH_F16, L.fat, L.lng, a1, FinNone())));
+        DslashArgs<VecF16, VecF32, VecF32> a2;
+        memset(&a2, 0, sizeof a2);
+        a2.out_par = par; a2.nsrc = 1; a2.skip = skip; a2.totals = tot;
+        a2.in[0].p = t16; a2.in[0].norm = t16n; a2.out[0].p = (float2 *)ttt; a2.p[0].p = (float2 *)cgp;
+        a2.r[0].p = (float2 *)r; a2.coef[0] = h.shift0;
+        MKS_TRY((launch_dslash<float, LinkF16, VecF16, VecF32, EPI_AXPY, 3>(MKS_K_DSLASH_F16, L.fat, L.lng, a2, FinMsAlpha{st})));
+      }
+      OpShiftUpdate<R> up;
+      memset(&up, 0, sizeof up);
+      for (int j = 0; j < nsh; j++) { up.psim[j] = psim[j]; up.pm[j] = pm[j]; }
+      up.r = r; up.ttt = ttt; up.cgp = cgp; up.p16 = p16; up.p16n = p16n; up.st = st; up.Vh = Vh;
+      MKS_TRY((launch_site<OpShiftUpdate<R>, 1, FinMsUpdate>(MKS_K_SHIFT, up, FinMsUpdate{st, skip}, skip, 1)));
+    }
+    MKS_CUDA(cudaMemcpyAsync(&h, st, sizeof h, cudaMemcpyDeviceToHost, c.stream));
+    MKS_CUDA(cudaStreamSynchronize(c.stream));
+    if (++guard > 10000000) return MKS_ERR_TIMEOUT;
+  }
+  *hstate = h;
+  return MKS_OK;
+}
+
+static int multishift_dev(const double *src_dev, double *const *psim_dev, const double *offsets, int nsh, int slot,
+                          const mks_invert_arg *arg, mks_invert_result *res) {
+  Context &c = ctx();
+  const LinkSlot &sl = c.slots[slot];
+  int par;
+  MKS_TRY(parity_index(arg->parity, &par));
+  for (int j = 0; j < nsh; j++)
+    if (!(offsets[j] > 0)) return MKS_ERR_ARG;  // ks_multicg_offset.c:152-158
+  double2 *src64;
+  MKS_TRY(wsv("ms_src64", 3 * c.Vh, &src64));
+  MKS_TRY(vec_aos_to_soa64(src_dev, src64, par));
+  const int niter = arg->max * arg->nrestart;
+  MsState h;
+  void *psim[MAXSH];
+  if (arg->prec == MKS_PREC_DOUBLE) {
+    MKS_TRY(multishift_core<double>(sl, par, MKS_PREC_DOUBLE, src64, nsh, offsets, arg->resid, niter, psim, &h));
+    for (int j = 0; j < nsh; j++) {
+      MKS_TRY(vec_soa64_to_aos((double2 *)psim[j], psim_dev[j], par));
+      res[j] = mks_invert_result();
+      res[j].final_rsq = h.rsq / (h.source_norm > 0 ? h.source_norm : 1.0);
+      res[j].size_r = res[j].final_rsq;
+      res[j].final_iters = h.iter;
+      res[j].converged = (h.source_norm == 0 || h.rsq <= h.rsqstop) ? 1 : 0;
+    }
+    if (h.source_norm == 0)
+      for (int j = 0; j < nsh; j++) MKS_TRY(vec_soa64_to_aos(src64, psim_dev[j], par));  // zero source -> zero
+    MKS_CUDA(cudaStreamSynchronize(c.stream));
+    return h.iter;
+  }
+  // sloppy multi-shift to at most 1e-5 (FP32 / FP16 vectors), then FP64-exact refinement of
+  // every shift by the mixed-precision CG (generic_ks/ks_multicg.c:170-228)
+  double sloppy_resid = arg->resid > 1e-5 ? arg->resid : 1e-5;
+  MKS_TRY(multishift_core<float>(sl, par, arg->prec, src64, nsh, offsets, sloppy_resid, niter, psim, &h));
+  int total_iters = h.iter;
+  for (int b0 = 0; b0 < nsh; b0 += MAXSRC) {
+    int nb = nsh - b0 < MAXSRC ? nsh - b0 : MAXSRC;
+    CgFields f;
+    memset(&f, 0, sizeof f);
+    MKS_TRY(alloc_cg_fields(f, nb, arg->prec));
+    OpF32ToF64 cv;
+    memset(&cv, 0, sizeof cv);
+    for (int s = 0; s < nb; s++) {
+      MKS_CUDA(cudaMemcpyAsync(f.src[s], src64, 3 * c.Vh * sizeof(double2), cudaMemcpyDeviceToDevice, c.stream));
+      cv.a[s] = (const float2 *)psim[b0 + s];
+      cv.b[s] = f.x[s];
+    }
+    cv.Vh = (int)c.Vh;
+    MKS_TRY((launch_site<OpF32ToF64, 0, FinNone>(MKS_K_BLAS, cv, FinNone(), nullptr, nb)));
+    double sig[MAXSRC];
+    for (int s = 0; s < nb; s++) sig[s] = offsets[b0 + s];
+    MKS_TRY(block_cg_shifted(slot, par, nb, sig, arg, f, res + b0));
+    for (int s = 0; s < nb; s++) {
+      MKS_TRY(vec_soa64_to_aos(f.x[s], psim_dev[b0 + s], par));
+      res[b0 + s].final_iters += total_iters;
+    }
+  }
+  MKS_CUDA(cudaStreamSynchronize(c.stream));
+  int mx = 0;
+  for (int j = 0; j < nsh; j++) mx = res[j].final_iters > mx ? res[j].final_iters : mx;
+  return mx;
+}
+
+}  // namespace mks
+
+extern "C" {
+
+int mks_ks_multicg_offset_field_dev(const double *src_dev, double *const *psim_dev, const double *offsets,
+                                    int num_offsets, int slot, const mks_invert_arg *arg, mks_invert_result *res) {
+  MKS_TRY(check_ready());
+  MKS_TRY(slot_ok(slot));
+  MKS_TRY(check_arg(arg, true));
+  if (num_offsets == 0) return 0;
+  if (num_offsets < 0 || num_offsets > MAXSH || !src_dev || !psim_dev || !offsets || !res) return MKS_ERR_ARG;
+  return multishift_dev(src_dev, psim_dev, offsets, num_offsets, slot, arg, res);
+}
+
+int mks_ks_multicg_offset_field(const double *src, double *const *psim, const double *offsets, int num_offsets,
+                                int slot, const mks_invert_arg *arg, mks_invert_result *res) {
+  MKS_TRY(check_ready());
+  MKS_TRY(slot_ok(slot));
+  MKS_TRY(check_arg(arg, true));
+  if (num_offsets == 0) return 0;
+  if (num_offsets < 0 || num_offsets > MAXSH || !src || !psim || !offsets || !res) return MKS_ERR_ARG;
+  Context &c = ctx();
+  size_t bytes = c.V * 6 * sizeof(double);
+  double *ds;
+  double *dp[MAXSH];
+  MKS_TRY(wsv("hsrc0", 6 * c.V, &ds));
+  MKS_CUDA(cudaMemcpyAsync(ds, src, bytes, cudaMemcpyHostToDevice, c.stream));
+  for (int j = 0; j < num_offsets; j++) {
+    MKS_TRY(wsv("hpsim" + std::to_string(j), 6 * c.V, &dp[j]));
+    MKS_CUDA(cudaMemcpyAsync(dp[j], psim[j], bytes, cudaMemcpyHostToDevice, c.stream));
+  }
+  int it = multishift_dev(ds, dp, offsets, num_offsets, slot, arg, res);
+  if (it < 0) return it;
+  for (int j = 0; j < num_offsets; j++)
+    MKS_CUDA(cudaMemcpyAsync(psim[j], dp[j], bytes, cudaMemcpyDeviceToHost, c.stream));
+  MKS_CUDA(cudaStreamSynchronize(c.stream));
+  return it;
+}
+
+}  // extern "C"

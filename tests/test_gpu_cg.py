@@ -1,0 +1,96 @@
+"""CG solvers on the GPU against the oracle (MILC's ks_congrad_parity semantics)."""
+import numpy as np
+import pytest
+
+from conftest import hisq_setup, rel
+
+pytestmark = pytest.mark.gpu
+
+DIMS = (8, 8, 8, 8)
+
+
+def _setup(m, oracle_cls, dims=DIMS):
+    U, orc, L = hisq_setup(m, oracle_cls, dims)
+    fat, lng = L["fat"][0], L["lng"][0]
+    m.set_lattice(dims)
+    m.load_fn_links(fat, lng)
+    return orc, fat, lng
+
+
+@pytest.mark.parametrize("parity", ["EVEN", "ODD"])
+def test_fp64_cg_matches_oracle(gpu, oracle_cls, parity):
+    m = gpu
+    orc, fat, lng = _setup(m, oracle_cls)
+    par = getattr(m, parity)
+    b = m.gen_vector(DIMS, 21, par)
+    x0 = m.gen_vector(DIMS, 22, par) * 0.1
+    qic = m.QuarkInvertControl(resid=1e-9, max=40, nrestart=10, parity=par, prec=m.PREC_DOUBLE)
+    x = x0.copy()
+    it = m.ks_congrad_parity(b, x, qic, 0.05)
+    it_o, xo, out = orc.congrad(fat, lng, b, x0, 0.05, par, 1e-9, 0.0, 40, 10)
+    # same algorithm, same restarts: identical iteration count, solution to rounding
+    assert it == it_o and qic.final_iters == int(out[4])
+    assert qic.final_restart == int(out[5]) and qic.converged == int(out[6]) == 1
+    assert rel(x, xo) < 1e-11
+    assert abs(qic.final_rsq - out[0]) <= 1e-6 * out[0]
+
+
+@pytest.mark.parametrize("prec", ["PREC_SINGLE", "PREC_HALF"])
+def test_mixed_cg_reaches_fp64_tolerance(gpu, oracle_cls, prec):
+    m = gpu
+    orc, fat, lng = _setup(m, oracle_cls)
+    b = m.gen_vector(DIMS, 31, m.EVEN)
+    qic = m.QuarkInvertControl(resid=1e-10, max=2000, nrestart=5, parity=m.EVEN, prec=getattr(m, prec))
+    x = np.zeros_like(b)
+    m.ks_congrad_parity(b, x, qic, 0.02)
+    assert qic.converged == 1 and qic.final_rsq < 1e-20
+    assert qic.reliable_updates >= 1
+    _, xo, _ = orc.congrad(fat, lng, b, np.zeros_like(b), 0.02, m.EVEN, 1e-13, 0.0, 2000, 5)
+    # |x - x*| / |x*| <= cond * |r|/|b|; at m=0.02 on these links the bound is ~1e-8
+    assert rel(x, xo) < 1e-7
+    # true residual recomputed here in FP64 through the oracle
+    Dx = orc.dslash(fat, lng, orc.dslash(fat, lng, x, m.ODD), m.EVEN)
+    r = b - (4 * 0.02 ** 2 * x - Dx)
+    V2 = b.shape[0] // 2
+    assert np.linalg.norm(r[:V2]) / np.linalg.norm(b[:V2]) < 1.01e-10
+
+
+def test_zero_source_gives_zero(gpu, oracle_cls):
+    m = gpu
+    _setup(m, oracle_cls)
+    b = np.zeros((int(np.prod(DIMS)), 6))
+    x = np.ones_like(b)
+    qic = m.QuarkInvertControl(resid=1e-8, parity=m.EVEN)
+    it = m.ks_congrad_parity(b, x, qic, 0.05)
+    V2 = b.shape[0] // 2
+    assert it == 0 and np.all(x[:V2] == 0) and np.all(x[V2:] == 1)
+
+
+@pytest.mark.parametrize("prec", ["PREC_DOUBLE", "PREC_SINGLE", "PREC_HALF"])
+@pytest.mark.parametrize("nsrc", [3, 8])
+def test_block_cg_each_source_matches_single(gpu, oracle_cls, prec, nsrc):
+    m = gpu
+    orc, fat, lng = _setup(m, oracle_cls)
+    srcs = [m.gen_vector(DIMS, 100 + k, m.EVEN) for k in range(nsrc)]
+    xs = [np.zeros_like(s) for s in srcs]
+    qic = m.QuarkInvertControl(resid=1e-10, max=2000, nrestart=5, parity=m.EVEN, prec=getattr(m, prec))
+    it, per = m.ks_congrad_block_parity(srcs, xs, qic, 0.02)
+    for k in range(nsrc):
+        assert per[k].converged == 1
+        _, xo, _ = orc.congrad(fat, lng, srcs[k], np.zeros_like(srcs[k]), 0.02, m.EVEN, 1e-13, 0.0, 2000, 5)
+        assert rel(xs[k], xo) < 1e-7, (k, rel(xs[k], xo))
+
+
+@pytest.mark.parametrize("prec", ["PREC_DOUBLE", "PREC_SINGLE"])
+def test_mat_invert_uml_matches_oracle(gpu, oracle_cls, prec):
+    m = gpu
+    orc, fat, lng = _setup(m, oracle_cls)
+    src = m.gen_vector(DIMS, 41, m.EVENANDODD)
+    x = np.zeros_like(src)
+    qic = m.QuarkInvertControl(resid=1e-10, max=1000, nrestart=5, prec=getattr(m, prec))
+    m.mat_invert_uml_field(src, x, qic, 0.05)
+    _, xo, _ = orc.mat_invert_uml(fat, lng, src, np.zeros_like(src), 0.05, 1e-12)
+    assert rel(x, xo) < 1e-8
+    # M x = src, checked with the oracle's D
+    Mx = 2 * 0.05 * x + orc.dslash(fat, lng, x, m.EVENANDODD)
+    assert rel(Mx, src) < 1e-9
