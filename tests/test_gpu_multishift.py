@@ -1,0 +1,58 @@
+"""Multi-shift CG on the GPU against the oracle (MILC's ks_multicg_offset_field)."""
+import numpy as np
+import pytest
+
+from conftest import hisq_setup, rel
+
+pytestmark = pytest.mark.gpu
+DIMS = (8, 8, 8, 8)
+
+
+def test_multishift_fp64_matches_oracle(gpu, oracle_cls):
+    m = gpu
+    U, orc, L = hisq_setup(m, oracle_cls, DIMS)
+    fat, lng = L["fat"][0], L["lng"][0]
+    m.set_lattice(DIMS)
+    m.load_fn_links(fat, lng)
+    b = m.gen_vector(DIMS, 51, m.EVEN)
+    offs = 4 * 0.02 ** 2 + np.logspace(-4, 0, 11)
+    psim = [np.zeros_like(b) for _ in offs]
+    qic = m.QuarkInvertControl(resid=1e-10, max=1000, nrestart=5, parity=m.EVEN, prec=m.PREC_DOUBLE)
+    it, per = m.ks_multicg_offset_field(b, psim, offs, qic)
+    it_o, po, fo = orc.multicg_offset(fat, lng, b, offs, m.EVEN, 1e-10)
+    assert abs(it - it_o) <= 1
+    for j in range(len(offs)):
+        assert rel(psim[j], po[j]) < 1e-9, (j, rel(psim[j], po[j]))
+        assert per[j].converged == 1
+
+
+@pytest.mark.parametrize("prec", ["PREC_SINGLE", "PREC_HALF"])
+def test_multishift_mixed_refined(gpu, oracle_cls, prec):
+    m = gpu
+    U, orc, L = hisq_setup(m, oracle_cls, DIMS)
+    fat, lng = L["fat"][0], L["lng"][0]
+    m.set_lattice(DIMS)
+    m.load_fn_links(fat, lng)
+    b = m.gen_vector(DIMS, 52, m.EVEN)
+    offs = np.logspace(-3, 0, 6)
+    psim = [np.zeros_like(b) for _ in offs]
+    qic = m.QuarkInvertControl(resid=1e-10, max=2000, nrestart=5, parity=m.EVEN, prec=getattr(m, prec))
+    it, per = m.ks_multicg_offset_field(b, psim, offs, qic)
+    for j, s in enumerate(offs):
+        # exact FP64 residual of each shifted system through the oracle
+        Dx = orc.dslash(fat, lng, orc.dslash(fat, lng, psim[j], m.ODD), m.EVEN)
+        r = b - (s * psim[j] - Dx)
+        V2 = b.shape[0] // 2
+        assert np.linalg.norm(r[:V2]) / np.linalg.norm(b[:V2]) < 1.01e-10, j
+        assert per[j].converged == 1
+
+
+def test_multishift_rejects_nonpositive_offset(gpu, oracle_cls):
+    m = gpu
+    U, orc, L = hisq_setup(m, oracle_cls, DIMS)
+    m.set_lattice(DIMS)
+    m.load_fn_links(L["fat"][0], L["lng"][0])
+    b = m.gen_vector(DIMS, 53, m.EVEN)
+    qic = m.QuarkInvertControl(resid=1e-8, parity=m.EVEN)
+    with pytest.raises(m.MksError):
+        m.ks_multicg_offset_field(b, [np.zeros_like(b)] * 2, [0.1, 0.0], qic)
