@@ -19,125 +19,10 @@
 #include <cstring>
 #include <vector>
 #include "mks_internal.cuh"
+#include "mks_su3.cuh"
 
 namespace mks {
 
-// a 3x3 matrix per site: element k of site (par,h) at p[par*ps + k*Vh + h]
-struct MatF {
-  double2 *p;
-  size_t ps;
-  __device__ __forceinline__ M3<double> ld(int par, int h, int Vh) const {
-    const double2 *b = p + par * ps + h;
-    M3<double> m;
-#pragma unroll
-    for (int k = 0; k < 9; k++) { double2 a = b[(size_t)k * Vh]; m.e[k / 3][k % 3] = {a.x, a.y}; }
-    return m;
-  }
-  __device__ __forceinline__ void st(int par, int h, int Vh, const M3<double> &m) const {
-    double2 *b = p + par * ps + h;
-#pragma unroll
-    for (int k = 0; k < 9; k++) b[(size_t)k * Vh] = make_double2(m.e[k / 3][k % 3].re, m.e[k / 3][k % 3].im);
-  }
-};
-
-__host__ __device__ static MatF link_dir(double2 *base, int dir, size_t Vh) { return {base + (size_t)dir * 9 * Vh, 36 * Vh}; }
-__host__ __device__ static MatF mat_field(double2 *base, size_t Vh) { return {base, 9 * Vh}; }
-
-__device__ __forceinline__ M3<double> mm_nn(const M3<double> &a, const M3<double> &b) {
-  M3<double> c;
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-      double re = 0, im = 0;
-#pragma unroll
-      for (int k = 0; k < 3; k++) {
-        re = fma(a.e[i][k].re, b.e[k][j].re, re); re = fma(-a.e[i][k].im, b.e[k][j].im, re);
-        im = fma(a.e[i][k].re, b.e[k][j].im, im); im = fma(a.e[i][k].im, b.e[k][j].re, im);
-      }
-      c.e[i][j] = {re, im};
-    }
-  return c;
-}
-__device__ __forceinline__ M3<double> mm_na(const M3<double> &a, const M3<double> &b) {  // a b^dag
-  M3<double> c;
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-      double re = 0, im = 0;
-#pragma unroll
-      for (int k = 0; k < 3; k++) {
-        re = fma(a.e[i][k].re, b.e[j][k].re, re); re = fma(a.e[i][k].im, b.e[j][k].im, re);
-        im = fma(a.e[i][k].im, b.e[j][k].re, im); im = fma(-a.e[i][k].re, b.e[j][k].im, im);
-      }
-      c.e[i][j] = {re, im};
-    }
-  return c;
-}
-__device__ __forceinline__ M3<double> mm_an(const M3<double> &a, const M3<double> &b) {  // a^dag b
-  M3<double> c;
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-      double re = 0, im = 0;
-#pragma unroll
-      for (int k = 0; k < 3; k++) {
-        re = fma(a.e[k][i].re, b.e[k][j].re, re); re = fma(a.e[k][i].im, b.e[k][j].im, re);
-        im = fma(a.e[k][i].re, b.e[k][j].im, im); im = fma(-a.e[k][i].im, b.e[k][j].re, im);
-      }
-      c.e[i][j] = {re, im};
-    }
-  return c;
-}
-
-// neighbour (checkerboard index) of site (par,h) displaced by d along mu
-__device__ __forceinline__ int nbr(const Geom &g, int par, int h, int mu, int d) {
-  int c[4];
-  site_coords(g, par, h, c[0], c[1], c[2], c[3]);
-  const int L[4] = {g.nx, g.ny, g.nz, g.nt};
-  c[mu] = wrap_add(c[mu], d, L[mu]);
-  return cb_index(g, c[0], c[1], c[2], c[3]);
-}
-__device__ __forceinline__ int nbr2(const Geom &g, int par, int h, int mu, int d1, int nu, int d2) {
-  int c[4];
-  site_coords(g, par, h, c[0], c[1], c[2], c[3]);
-  const int L[4] = {g.nx, g.ny, g.nz, g.nt};
-  c[mu] = wrap_add(c[mu], d1, L[mu]);
-  c[nu] = wrap_add(c[nu], d2, L[nu]);
-  return cb_index(g, c[0], c[1], c[2], c[3]);
-}
-
-// fat_mu(x) += coef * S(x); S saved when sout.p != nullptr
-__global__ void __launch_bounds__(128) k_staple(Geom g, int mu, int nu, MatF Unu, MatF A, MatF fat, double coef,
-                                                MatF sout) {
-  const int h = blockIdx.x * blockDim.x + threadIdx.x;
-  const int par = blockIdx.y, opar = 1 - par;
-  const int Vh = g.Vh;
-  if (h >= Vh) return;
-  const int xpnu = nbr(g, par, h, nu, 1), xpmu = nbr(g, par, h, mu, 1), xmnu = nbr(g, par, h, nu, -1);
-  const int xmnupmu = nbr2(g, par, h, nu, -1, mu, 1);
-  // upper: U_nu(x) [A(x+nu) U_nu(x+mu)^dag]
-  M3<double> up = mm_nn(Unu.ld(par, h, Vh), mm_na(A.ld(opar, xpnu, Vh), Unu.ld(opar, xpmu, Vh)));
-  // lower: [U_nu(x-nu)^dag A(x-nu)] U_nu(x-nu+mu)
-  M3<double> dn = mm_nn(mm_an(Unu.ld(opar, xmnu, Vh), A.ld(opar, xmnu, Vh)), Unu.ld(par, xmnupmu, Vh));
-  M3<double> s;
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) s.e[i][j] = {up.e[i][j].re + dn.e[i][j].re, up.e[i][j].im + dn.e[i][j].im};
-  M3<double> f = fat.ld(par, h, Vh);
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-      f.e[i][j].re += coef * s.e[i][j].re;
-      f.e[i][j].im += coef * s.e[i][j].im;
-    }
-  fat.st(par, h, Vh, f);
-  if (sout.p) sout.st(par, h, Vh, s);
-}
 
 // out = a * in (all four directions, both parities)
 __global__ void k_scale_links(const double2 *in, double2 *out, double a, size_t n) {
