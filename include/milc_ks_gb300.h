@@ -194,11 +194,19 @@ int mks_hisq_reunit_svd_count(void);
  * :1182-1475): mom[dir](x) += TA( +-2 eps U_mu(x) dS/dU_mu(x) ) for the
  * rational-function terms sum_j residues[j] |xxx_j><xxx_j| with xxx_j = X_j
  * on even sites and D_oe X_j on odd sites.  n_orders_naik[g] gives how many
- * consecutive terms belong to Naik group g (the first group counts every
- * term).  Uses the aux links of the last mks_load_links_from_thin. */
+ * consecutive terms belong to Naik group g (MILC's n_orders_naik[],
+ * ks_imp_rhmc/setup.c:295-339; the counts add up to nterms): every term
+ * goes through the level-2 smearing, and the terms of group g >= 1 also
+ * through eps_naik[g] (1-link + Naik) of that group's links.  Uses the aux
+ * links U, V, W of the last mks_load_links_from_thin (HISQ action). */
 int mks_fermion_force_multi_hisq(double eps, const double *residues,
                                  const double *const *xxx, int nterms,
                                  const int *n_orders_naik, int n_naiks, double *mom);
+/* FP64 flops of the adjoint kernels in the last force call (our count:
+   198 per 3x3 complex matrix product), and the number of links where the
+   eigenvalue filter (generic_ks/su3_mat_op.c:1680-1734) was applied. */
+double mks_force_flops_last(void);
+int mks_force_filter_count(void);
 
 /* ------------------------------------------------------------------ */
 /* Kernel timing.  When enabled, the library brackets every launch of its

@@ -70,6 +70,8 @@ SIGNATURES = {
     "mks_get_hisq_aux": (ctypes.c_int, [DP, DP]),
     "mks_hisq_reunit_svd_count": (ctypes.c_int, []),
     "mks_fermion_force_multi_hisq": (ctypes.c_int, [ctypes.c_double, DP, DPP, ctypes.c_int, IP, ctypes.c_int, DP]),
+    "mks_force_flops_last": (ctypes.c_double, []),
+    "mks_force_filter_count": (ctypes.c_int, []),
     "mks_timing_enable": (ctypes.c_int, [ctypes.c_int]),
     "mks_timing_reset": (ctypes.c_int, []),
     "mks_timing_get": (ctypes.c_int, [ctypes.c_int, DP, ctypes.POINTER(ctypes.c_longlong)]),

