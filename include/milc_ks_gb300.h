@@ -187,6 +187,21 @@ int mks_get_hisq_aux(double *V, double *W);
    the analytic projection was used for them.  Returns a count >= 0. */
 int mks_hisq_reunit_svd_count(void);
 
+/* Generic-coefficient loaders, one per MILC GPU loader:
+ * coeffs = {one_link, naik, three_staple, five_staple, seven_staple, lepage}
+ * as in MILC's asqtad_coeffs_t (include/ks_action_paths.h:23-30).
+ *  - mks_fatlong_links replaces load_fatlinks_gpu / load_fatlonglinks_gpu
+ *    (generic_ks/fermion_links_fn_load_gpu.c:19-78): fat (and, when lng is
+ *    not NULL, long) links of `links` by the optimised staple recursion
+ *    (fermion_links_fn_load_milc.c:207-253) and the Naik path.
+ *  - mks_hisq_aux_links replaces load_hisq_aux_links_gpu (:80-110): V =
+ *    fat(U; coeffs1), W = U(3) projection of V; U, V, W stay resident for
+ *    the force and are copied back when V / W are not NULL.
+ *  - mks_load_hisq_aux uploads U, V, W built elsewhere for the force. */
+int mks_fatlong_links(const double coeffs[6], const double *links, double *fat, double *lng);
+int mks_hisq_aux_links(const double coeffs1[6], const double *U, double *V, double *W);
+int mks_load_hisq_aux(const double *U, const double *V, const double *W);
+
 /* ------------------------------------------------------------------ */
 /* HISQ fermion force.  Replaces eo_fermion_force_multi with the GPU
  * wrapper fn_fermion_force_multi_hisq_wrapper_mx_gpu

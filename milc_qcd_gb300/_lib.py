@@ -69,6 +69,9 @@ SIGNATURES = {
     "mks_load_links_from_thin": (ctypes.c_int, [ctypes.c_int, DP, ctypes.c_int, DP, ctypes.c_double]),
     "mks_get_hisq_aux": (ctypes.c_int, [DP, DP]),
     "mks_hisq_reunit_svd_count": (ctypes.c_int, []),
+    "mks_fatlong_links": (ctypes.c_int, [DP, DP, DP, DP]),
+    "mks_hisq_aux_links": (ctypes.c_int, [DP, DP, DP, DP]),
+    "mks_load_hisq_aux": (ctypes.c_int, [DP, DP, DP]),
     "mks_fermion_force_multi_hisq": (ctypes.c_int, [ctypes.c_double, DP, DPP, ctypes.c_int, IP, ctypes.c_int, DP]),
     "mks_force_flops_last": (ctypes.c_double, []),
     "mks_force_filter_count": (ctypes.c_int, []),

@@ -298,3 +298,112 @@ int mks_get_hisq_aux(double *V, double *W) {
 }
 
 }  // extern "C"
+
+// --------------------------------------------------------------------
+// Generic-coefficient entry points, one per MILC loader the drop-in
+// replaces (generic_ks/fermion_links_fn_load_gpu.c:19-110).
+namespace mks {
+
+static int ensure_aux() {
+  Context &c = ctx();
+  size_t nall = 8 * 9 * c.Vh;
+  if (!c.auxU) {
+    MKS_TRY(dev_alloc((void **)&c.auxU, nall * sizeof(double2)));
+    MKS_TRY(dev_alloc((void **)&c.auxV, nall * sizeof(double2)));
+    MKS_TRY(dev_alloc((void **)&c.auxW, nall * sizeof(double2)));
+  }
+  return MKS_OK;
+}
+
+static int to_host(const double2 *soa, double *host, double *stage) {
+  Context &c = ctx();
+  MKS_TRY(links_soa64_to_aos(soa, stage));
+  MKS_CUDA(cudaMemcpyAsync(host, stage, c.V * 72 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  MKS_CUDA(cudaStreamSynchronize(c.stream));
+  return MKS_OK;
+}
+
+}  // namespace mks
+
+extern "C" {
+
+int mks_fatlong_links(const double coeffs[6], const double *links, double *fat, double *lng) {
+  MKS_TRY(check_ready());
+  if (!coeffs || !links || (!fat && !lng)) return MKS_ERR_ARG;
+  Context &c = ctx();
+  const size_t Vh = c.Vh, nall = 8 * 9 * Vh, bytes = c.V * 72 * sizeof(double);
+  const FatCoeffs cf = {coeffs[0], coeffs[1], coeffs[2], coeffs[3], coeffs[4], coeffs[5]};
+  double *stage = nullptr;
+  double2 *L = nullptr, *F = nullptr, *S = nullptr, *T = nullptr;
+  int rc = dev_alloc((void **)&stage, bytes);
+  if (rc >= 0) rc = dev_alloc((void **)&L, nall * sizeof(double2));
+  if (rc >= 0) rc = dev_alloc((void **)&F, nall * sizeof(double2));
+  if (rc >= 0) rc = dev_alloc((void **)&S, 2 * 9 * Vh * sizeof(double2));
+  if (rc >= 0) rc = dev_alloc((void **)&T, 2 * 9 * Vh * sizeof(double2));
+  if (rc >= 0 && cudaMemcpyAsync(stage, links, bytes, cudaMemcpyHostToDevice, c.stream) != cudaSuccess)
+    rc = MKS_ERR_CUDA;
+  if (rc >= 0) rc = links_aos_to_soa64(stage, L);
+  if (rc >= 0 && fat) rc = fatten(L, cf, F, S, T);
+  if (rc >= 0 && fat) rc = to_host(F, fat, stage);
+  if (rc >= 0 && lng) rc = naik(L, F, cf.naik);
+  if (rc >= 0 && lng) rc = to_host(F, lng, stage);
+  cudaStreamSynchronize(c.stream);
+  dev_free(stage); dev_free(L); dev_free(F); dev_free(S); dev_free(T);
+  return rc;
+}
+
+int mks_hisq_aux_links(const double coeffs1[6], const double *U, double *V, double *W) {
+  MKS_TRY(check_ready());
+  if (!coeffs1 || !U) return MKS_ERR_ARG;
+  Context &c = ctx();
+  const size_t Vh = c.Vh, bytes = c.V * 72 * sizeof(double);
+  const FatCoeffs cf = {coeffs1[0], coeffs1[1], coeffs1[2], coeffs1[3], coeffs1[4], coeffs1[5]};
+  MKS_TRY(ensure_aux());
+  double *stage = nullptr;
+  double2 *S = nullptr, *T = nullptr;
+  unsigned int *nsvd = nullptr;
+  int rc = dev_alloc((void **)&stage, bytes);
+  if (rc >= 0) rc = dev_alloc((void **)&S, 2 * 9 * Vh * sizeof(double2));
+  if (rc >= 0) rc = dev_alloc((void **)&T, 2 * 9 * Vh * sizeof(double2));
+  if (rc >= 0) rc = dev_alloc((void **)&nsvd, sizeof(unsigned int));
+  if (rc >= 0 && cudaMemsetAsync(nsvd, 0, sizeof(unsigned int), c.stream) != cudaSuccess) rc = MKS_ERR_CUDA;
+  if (rc >= 0 && cudaMemcpyAsync(stage, U, bytes, cudaMemcpyHostToDevice, c.stream) != cudaSuccess)
+    rc = MKS_ERR_CUDA;
+  if (rc >= 0) rc = links_aos_to_soa64(stage, c.auxU);
+  if (rc >= 0) rc = fatten(c.auxU, cf, c.auxV, S, T);
+  if (rc >= 0) {
+    timing_begin(MKS_K_LINKS);
+    k_unitarize<<<dim3(grid_for(Vh, 128), 2, 4), 128, 0, c.stream>>>(c.geom, c.auxV, c.auxW, nsvd);
+    timing_end(MKS_K_LINKS);
+    if (cudaGetLastError() != cudaSuccess) rc = MKS_ERR_CUDA;
+  }
+  if (rc >= 0 && cudaMemcpyAsync(&g_nsvd, nsvd, sizeof(unsigned int), cudaMemcpyDeviceToHost, c.stream) != cudaSuccess)
+    rc = MKS_ERR_CUDA;
+  if (rc >= 0 && V) rc = to_host(c.auxV, V, stage);
+  if (rc >= 0 && W) rc = to_host(c.auxW, W, stage);
+  cudaStreamSynchronize(c.stream);
+  dev_free(stage); dev_free(S); dev_free(T); dev_free(nsvd);
+  return rc;
+}
+
+int mks_load_hisq_aux(const double *U, const double *V, const double *W) {
+  MKS_TRY(check_ready());
+  if (!U || !V || !W) return MKS_ERR_ARG;
+  Context &c = ctx();
+  const size_t bytes = c.V * 72 * sizeof(double);
+  MKS_TRY(ensure_aux());
+  double *stage = nullptr;
+  MKS_TRY(dev_alloc((void **)&stage, bytes));
+  const double *src[3] = {U, V, W};
+  double2 *dst[3] = {c.auxU, c.auxV, c.auxW};
+  int rc = MKS_OK;
+  for (int k = 0; k < 3 && rc >= 0; k++) {
+    if (cudaMemcpyAsync(stage, src[k], bytes, cudaMemcpyHostToDevice, c.stream) != cudaSuccess) rc = MKS_ERR_CUDA;
+    if (rc >= 0) rc = links_aos_to_soa64(stage, dst[k]);
+    if (rc >= 0 && cudaStreamSynchronize(c.stream) != cudaSuccess) rc = MKS_ERR_CUDA;
+  }
+  dev_free(stage);
+  return rc;
+}
+
+}  // extern "C"

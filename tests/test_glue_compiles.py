@@ -1,0 +1,40 @@
+"""The MILC-side binding (milc_qcd_gb300/milc_glue/mks_milc_glue.c) compiles
+against MILC's headers, and so do the MILC files the USE_*_GPU macro swaps
+touch.  Needs the reference tree; skipped elsewhere."""
+import os
+import subprocess
+
+import pytest
+
+from conftest import ROOT
+
+REF = "/root/reference"
+pytestmark = pytest.mark.skipif(not os.path.isdir(REF), reason="reference tree not present")
+
+FLAGS = ["-fsyntax-only", "-std=gnu99", "-w", "-DMILC_PRECISION=2", "-DFN", "-DHMC", "-DHISQ_FF_MULTI_WRAPPER",
+         "-DSINGLE", "-DINT_ALG=INT_3G1F", "-DKS_MULTICG=HYBRID", "-DKS_MULTIFF=FNMAT", "-DFEWSUMS",
+         "-DDBLSTORE_FN", "-DUSE_CG_GPU", "-DUSE_FL_GPU", "-DUSE_FF_GPU",
+         "-include", os.path.join(ROOT, "milc_qcd_gb300", "milc_glue", "mks_milc_alloc.h")]
+
+
+def _inc(tmp_path):
+    inc = tmp_path / "inc"
+    inc.mkdir()
+    (inc / "quark_action.h").write_text('#include "%s/generic_ks/imp_actions/hisq/hisq_u3_action.h"\n' % REF)
+    (inc / "gauge_action.h").write_text('#include "%s/generic/imp_actions/symanzik_1loop_hisq_action.h"\n' % REF)
+    return ["-I" + str(inc), "-I" + REF + "/ks_imp_rhmc", "-I" + REF + "/include", "-I" + REF + "/generic_ks",
+            "-I" + os.path.join(ROOT, "include")]
+
+
+@pytest.mark.parametrize("src", [
+    os.path.join(ROOT, "milc_qcd_gb300", "milc_glue", "mks_milc_glue.c"),
+    REF + "/generic_ks/fermion_links_hisq_load_milc.c",
+    REF + "/generic_ks/fn_links_milc.c",
+    REF + "/generic_ks/fermion_links_from_site.c",
+    REF + "/generic_ks/d_congrad5_fn.c",
+    REF + "/generic_ks/ks_multicg.c",
+    REF + "/generic_ks/mat_invert.c",
+])
+def test_compiles(tmp_path, src):
+    r = subprocess.run(["gcc"] + FLAGS + _inc(tmp_path) + [src], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
