@@ -114,6 +114,20 @@ int mks_get_fn_links(int slot, double *fat, double *lng);
  * D src, src read on the other parity.  parity may be MKS_EVENANDODD. */
 int mks_dslash_fn_field(const double *src, double *dst, int parity, int slot);
 int mks_dslash_fn_field_dev(const double *src_dev, double *dst_dev, int parity, int slot);
+/* The same D_eo for callers that cannot allocate device memory (no
+ * counterpart in the reference; MILC's own paths allocate freely).
+ * mks_dslash_fn_field_dev allocates its staging buffers with cudaMalloc on
+ * first use; an application that gives nearly all device memory to its own
+ * pool allocator, or code that must not run a device-wide synchronising
+ * call such as cudaMalloc at that moment, calls this variant instead.  It
+ * allocates nothing: its staging lives in a fixed 32 MiB device array that
+ * every GPU loading the library keeps until exit, which limits it to
+ * lattices of at most 349,525 sites (MKS_ERR_ARG beyond).  All calls share
+ * that array; calls that overlap on the GPU race on it.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress); make
+ * that first call before any stream capture.  Links must already be loaded
+ * in `slot`. */
+int mks_dslash_fn_field_dev_noalloc(const double *src_dev, double *dst_dev, int parity, int slot);
 
 /* ------------------------------------------------------------------ */
 /* Single-source CG on (4m^2 - D_eo D_oe) for one parity.

@@ -47,6 +47,8 @@ SIGNATURES = {
     "mks_get_fn_links": (ctypes.c_int, [ctypes.c_int, DP, DP]),
     "mks_dslash_fn_field": (ctypes.c_int, [DP, DP, ctypes.c_int, ctypes.c_int]),
     "mks_dslash_fn_field_dev": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "mks_dslash_fn_field_dev_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                                       ctypes.c_int]),
     "mks_ks_congrad_parity": (ctypes.c_int, [DP, DP, ctypes.c_double, ctypes.c_int,
                                              ctypes.POINTER(InvertArg), ctypes.POINTER(InvertResult)]),
     "mks_ks_congrad_parity_dev": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
