@@ -89,6 +89,18 @@ def dist_env():
     return rank, world
 
 
+def max_over_ranks(value, world, device="cpu"):
+    """The slowest rank's step time: the path has no data-path collective
+    (one independent replica per GPU), only this timing reduction."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 # ---------------------------------------------------------------- reference arm
 def cpu_baseline(sample_iters=20, threads=None):
     """MILC's CG (the C oracle restatement of d_congrad5_fn_milc.c) on the host
@@ -206,10 +218,7 @@ def gpu_arm(args):
     lib.mks_timing_enable(0)
     launches = lib.mks_launch_count() - launches0
     step_ms = ev0.elapsed_time(ev1) / args.steps
-    if world > 1:
-        t = torch.tensor([step_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        step_ms = float(t.item())
+    step_ms = max_over_ranks(step_ms, world, "cuda")
     per_src = step_ms / 1e3 / N
     reliable = [res[k].reliable_updates for k in range(N)]
     # verify every solution in FP64 on the GPU: r = b - M^dag M x with the FP64 operator
@@ -220,6 +229,12 @@ def gpu_arm(args):
     fam = {m.PREC_HALF: 2, m.PREC_SINGLE: 1, m.PREC_DOUBLE: 0}[prec]
     if N > 1 and prec != m.PREC_DOUBLE:
         fam = 3
+    kernel_ms = {}
+    for name, k in _lib.KERNEL_FAMILIES.items():
+        t, n = ctypes.c_double(), ctypes.c_longlong()
+        lib.mks_timing_get(k, ctypes.byref(t), ctypes.byref(n))
+        if n.value:
+            kernel_ms[name] = {"ms_per_step": t.value / args.steps, "launches_per_step": n.value / args.steps}
     tot_ms, nl = ctypes.c_double(), ctypes.c_longlong()
     lib.mks_timing_get(fam, ctypes.byref(tot_ms), ctypes.byref(nl))
     dslash_ms = tot_ms.value / max(nl.value, 1)
@@ -279,6 +294,7 @@ def gpu_arm(args):
         "e2e": {"value": e2e_per_src, "unit": "s/solve", "h2d_bytes_per_step": 2 * N * bytes_field,
                 "d2h_bytes_per_step": N * bytes_field},
         "gpu_launches": int(launches),
+        "kernel_ms": kernel_ms,
         "clocks": clk.summary(),
         "link_build_s": t_links,
     }

@@ -248,7 +248,8 @@ int mks_force_filter_count(void);
 #define MKS_K_SHIFT        5
 #define MKS_K_LINKS        6
 #define MKS_K_FORCE        7
-#define MKS_K_COUNT        8
+#define MKS_K_TUNE         8   /* autotuner trial launches */
+#define MKS_K_COUNT        9
 int mks_timing_enable(int on);
 int mks_timing_reset(void);
 int mks_timing_get(int family, double *total_ms, long long *launches);
@@ -265,6 +266,13 @@ void *mks_stream(void);
  * nsrc > 1 times the multi-source kernel. */
 int mks_bench_dslash(int prec, int nsrc, int parity, int slot, int iters, int flush_l2,
                      double *ms);
+
+/* D_eo launch shape chosen by the autotuner for (prec, nsrc): G threads per
+ * site, nb sources per thread, block threads per CTA.  The tuner times
+ * every candidate on the live links the first time a (prec, nsrc) pair is
+ * launched (environment MKS_TUNE=0 keeps a fixed table).  Returns
+ * MKS_ERR_STATE when the pair has not been launched yet. */
+int mks_tuned_shape(int prec, int nsrc, int *G, int *nb, int *block);
 
 /* ------------------------------------------------------------------ */
 /* Host-side synthetic inputs (no device work).  See mks_fields.c. */

@@ -15,7 +15,7 @@ MKS_PREC_HALF, MKS_PREC_SINGLE, MKS_PREC_DOUBLE = 0, 1, 2
 MKS_ACTION_HISQ, MKS_ACTION_ASQTAD = 1, 2
 MKS_MAX_SLOTS = 12
 KERNEL_FAMILIES = {"dslash_f64": 0, "dslash_f32": 1, "dslash_f16": 2, "dslash_mrhs": 3, "blas": 4,
-                   "shift": 5, "links": 6, "force": 7}
+                   "shift": 5, "links": 6, "force": 7, "tune": 8}
 
 
 class InvertArg(ctypes.Structure):
@@ -84,6 +84,7 @@ SIGNATURES = {
     "mks_stream": (ctypes.c_void_p, []),
     "mks_bench_dslash": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_int, DP]),
+    "mks_tuned_shape": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, IP, IP, IP]),
     "mks_site_coords": (None, [IP, ctypes.c_size_t, IP]),
     "mks_site_index": (ctypes.c_size_t, [IP, IP]),
     "mks_staggered_phase": (ctypes.c_double, [IP, IP, ctypes.c_int]),

@@ -393,6 +393,7 @@ int force_dev(double eps, const double *residues, double2 *const *xs, int nterms
               double *mom_dev) {
   Context &c = ctx();
   const size_t Vh = c.Vh, nl = 8 * 9 * Vh, nm = 2 * 9 * Vh;
+  g_force_flops = 0.0;
   const ForceCoeffs c1 = {1.0 / 8.0, 0.0, -1.0 / 16.0, 1.0 / 64.0, -1.0 / 384.0, 0.0};
   const ForceCoeffs c2 = {1.0 / 8.0 + 2.0 * 6.0 / 16.0 + 1.0 / 8.0, -1.0 / 24.0, -1.0 / 16.0, 1.0 / 64.0,
                           -1.0 / 384.0, -2.0 / 16.0};

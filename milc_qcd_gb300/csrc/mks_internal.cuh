@@ -154,7 +154,7 @@ struct VecF16 {
     float s = __ldg(norm + h);
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-      float2 a = __half22float2(p[(size_t)c * Vh + h]);
+      float2 a = __half22float2(__ldg(p + (size_t)c * Vh + h));
       v.c[c] = {a.x * s, a.y * s};
     }
     return v;
@@ -216,7 +216,7 @@ struct LinkF16 {
         m.e[e / 3][e % 3] = {f.x * scale, f.y * scale};
       }
     }
-    float2 f = __half22float2(b[(size_t)(par * 4 + dir) * Vh + h]);
+    float2 f = __half22float2(__ldg(b + (size_t)(par * 4 + dir) * Vh + h));
     m.e[2][2] = {f.x * scale, f.y * scale};
     return m;
   }

@@ -337,22 +337,35 @@ static LinkSet16 links16(const LinkSlot &s) {
   return {{s.fat16a, s.fat16b, s.fat16scale}, {s.lng16a, s.lng16b, s.lng16scale}};
 }
 
-// thread-group shape for nsrc sources: G threads per site, NB sources each
-struct Shape { int G, NB; };
-static Shape shape_for(int nsrc) {
-  if (nsrc <= 1) return {1, 1};
-  if (nsrc <= 2) return {1, 2};
-  if (nsrc <= 4) return {1, 4};
-  if (nsrc <= 8) return {2, 4};
-  return {4, 4};
+// ------------------------------------------------------------------
+// D_eo launch shapes and their autotuner.
+// A shape is (G threads per site, NB sources per thread, block size).  The
+// first launch for a given (link precision, nsrc) times every candidate
+// with G*NB >= nsrc (and at most 2x padding) on the live links and scratch
+// vectors, keeps the fastest, and reuses it for every epilogue.  MKS_TUNE=0
+// turns tuning off (fixed table); the choices can be read back with
+// mks_tuned_shape().
+struct Shape { int G, NB, block; };
+static Shape g_shape[3][MAXSRC + 1];  // [prec][nsrc], G == 0: not chosen yet
+
+static Shape default_shape(int nsrc) {
+  if (nsrc <= 1) return {1, 1, 256};
+  if (nsrc <= 2) return {1, 2, 256};
+  if (nsrc <= 4) return {1, 4, 256};
+  if (nsrc <= 8) return {2, 4, 256};
+  return {4, 4, 256};
 }
+
+template <class LinkT> struct PrecOf;
+template <> struct PrecOf<LinkF64> { enum { v = MKS_PREC_DOUBLE }; typedef VecF64 In; typedef VecF64 Out; typedef double R; };
+template <> struct PrecOf<LinkF32> { enum { v = MKS_PREC_SINGLE }; typedef VecF32 In; typedef VecF32 Out; typedef float R; };
+template <> struct PrecOf<LinkF16> { enum { v = MKS_PREC_HALF }; typedef VecF16 In; typedef VecF32 Out; typedef float R; };
 
 template <typename R, class LinkT, class InT, class OutT, int NB, int EPI, int NSUM, class Fin>
 static int launch_dslash_nb(int family, const LinkT &fat, const LinkT &lng,
-                            DslashArgs<InT, OutT, typename EpiLoad<R>::type> &a, const Fin &fin) {
+                            DslashArgs<InT, OutT, typename EpiLoad<R>::type> &a, const Fin &fin, int block) {
   Context &c = ctx();
   size_t threads = (size_t)c.Vh * a.groups;
-  int block = 256;
   int grid = (int)((threads + block - 1) / block);
   if (NSUM > 0) {
     MKS_TRY(ensure_red(NSUM * a.groups * NB, grid));
@@ -367,17 +380,103 @@ static int launch_dslash_nb(int family, const LinkT &fat, const LinkT &lng,
 }
 
 template <typename R, class LinkT, class InT, class OutT, int EPI, int NSUM, class Fin>
-static int launch_dslash(int family, const LinkT &fat, const LinkT &lng,
-                         DslashArgs<InT, OutT, typename EpiLoad<R>::type> &a, const Fin &fin) {
-  Shape sh = shape_for(a.nsrc);
+static int launch_shape(int family, const LinkT &fat, const LinkT &lng,
+                        DslashArgs<InT, OutT, typename EpiLoad<R>::type> &a, const Fin &fin, const Shape &sh) {
   a.groups = sh.G;
   a.g = ctx().geom;
-  if (a.nsrc > 1 && family != MKS_K_DSLASH_F64) family = MKS_K_DSLASH_MRHS;
   switch (sh.NB) {
-  case 1: return launch_dslash_nb<R, LinkT, InT, OutT, 1, EPI, NSUM, Fin>(family, fat, lng, a, fin);
-  case 2: return launch_dslash_nb<R, LinkT, InT, OutT, 2, EPI, NSUM, Fin>(family, fat, lng, a, fin);
-  default: return launch_dslash_nb<R, LinkT, InT, OutT, 4, EPI, NSUM, Fin>(family, fat, lng, a, fin);
+  case 1: return launch_dslash_nb<R, LinkT, InT, OutT, 1, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block);
+  case 2: return launch_dslash_nb<R, LinkT, InT, OutT, 2, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block);
+  case 4: return launch_dslash_nb<R, LinkT, InT, OutT, 4, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block);
+  default: return launch_dslash_nb<R, LinkT, InT, OutT, 8, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block);
   }
+}
+
+__global__ void k_fill_tune(float *v, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    v[i] = 0.25f * (float)((i * 2654435761u) >> 24 & 255) / 255.0f;
+}
+
+static bool tuning_enabled() {
+  static int v = -1;
+  if (v < 0) {
+    const char *e = getenv("MKS_TUNE");
+    v = e ? atoi(e) : 1;
+  }
+  return v != 0;
+}
+
+static void set_vec(VecF64 &v, float *p, float *) { v.p = (double2 *)p; }
+static void set_vec(VecF32 &v, float *p, float *) { v.p = (float2 *)p; }
+static void set_vec(VecF16 &v, float *p, float *n) { v.p = (__half2 *)p; v.norm = n; }
+
+template <class LinkT>
+static int tune_shape(const LinkT &fat, const LinkT &lng, int nsrc, Shape *best) {
+  typedef PrecOf<LinkT> P;
+  typedef typename P::R R;
+  typedef typename P::In InT;
+  typedef typename P::Out OutT;
+  Context &c = ctx();
+  *best = default_shape(nsrc);
+  if (!tuning_enabled()) return MKS_OK;
+  const size_t n = 3 * c.Vh;
+  DslashArgs<InT, OutT, typename EpiLoad<R>::type> a;
+  memset(&a, 0, sizeof a);
+  a.nsrc = nsrc;
+  a.out_par = 0;
+  for (int s = 0; s < nsrc; s++) {
+    float *in, *out, *nrm;
+    MKS_TRY(wsv("tune_in" + std::to_string(s), n * 4, &in));     // large enough for any precision
+    MKS_TRY(wsv("tune_out" + std::to_string(s), n * 4, &out));
+    MKS_TRY(wsv("tune_nrm" + std::to_string(s), c.Vh, &nrm));
+    k_fill_tune<<<c.sm_count * 4, 256, 0, c.stream>>>(in, n * 4);
+    k_fill_tune<<<c.sm_count * 4, 256, 0, c.stream>>>(nrm, c.Vh);
+    set_vec(a.in[s], in, nrm);
+    set_vec(a.out[s], out, nrm);
+  }
+  MKS_CUDA(cudaGetLastError());
+  cudaEvent_t e0, e1;
+  MKS_CUDA(cudaEventCreate(&e0));
+  MKS_CUDA(cudaEventCreate(&e1));
+  float best_ms = 1e30f;
+  const int nbs[4] = {1, 2, 4, 8};
+  for (int ib = 0; ib < 4; ib++) {
+    for (int G = 1; G <= 16; G *= 2) {
+      const int NB = nbs[ib];
+      if (G * NB < nsrc || G * NB > MAXSRC || (G * NB >= 2 * nsrc && G * NB > 1)) continue;
+      for (int block = 128; block <= 256; block *= 2) {
+        Shape sh = {G, NB, block};
+        float tot = 0;
+        for (int it = 0; it < 4; it++) {
+          MKS_CUDA(cudaEventRecord(e0, c.stream));
+          MKS_TRY((launch_shape<R, LinkT, InT, OutT, EPI_PLAIN, 0>(MKS_K_TUNE, fat, lng, a, NoFinish(), sh)));
+          MKS_CUDA(cudaEventRecord(e1, c.stream));
+          MKS_CUDA(cudaEventSynchronize(e1));
+          float ms;
+          MKS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+          if (it > 0) tot += ms;
+        }
+        if (tot < best_ms) { best_ms = tot; *best = sh; }
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return MKS_OK;
+}
+
+template <typename R, class LinkT, class InT, class OutT, int EPI, int NSUM, class Fin>
+static int launch_dslash(int family, const LinkT &fat, const LinkT &lng,
+                         DslashArgs<InT, OutT, typename EpiLoad<R>::type> &a, const Fin &fin) {
+  const int pk = PrecOf<LinkT>::v;
+  Shape &sh = g_shape[pk][a.nsrc];
+  if (sh.G == 0) {
+    Shape t;
+    MKS_TRY(tune_shape(fat, lng, a.nsrc, &t));
+    sh = t;
+  }
+  if (a.nsrc > 1 && family != MKS_K_DSLASH_F64) family = MKS_K_DSLASH_MRHS;
+  return launch_shape<R, LinkT, InT, OutT, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh);
 }
 
 // plain D on FP64 SoA fields, nsrc sources
@@ -1515,3 +1614,13 @@ int mks_ks_multicg_offset_field(const double *src, double *const *psim, const do
 }
 
 }  // extern "C"
+
+extern "C" int mks_tuned_shape(int prec, int nsrc, int *G, int *nb, int *block) {
+  if (prec < 0 || prec > 2 || nsrc < 1 || nsrc > MAXSRC) return MKS_ERR_ARG;
+  const Shape &s = g_shape[prec][nsrc];
+  if (s.G == 0) return MKS_ERR_STATE;
+  if (G) *G = s.G;
+  if (nb) *nb = s.NB;
+  if (block) *block = s.block;
+  return MKS_OK;
+}
