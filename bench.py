@@ -202,6 +202,7 @@ def gpu_arm(args):
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
+    launches_before = lib.mks_launch_count()  # library kernels since mks_init (for ncu -s)
     lib.mks_timing_reset()
     lib.mks_timing_enable(1)
     launches0 = lib.mks_launch_count()
@@ -294,6 +295,7 @@ def gpu_arm(args):
         "e2e": {"value": e2e_per_src, "unit": "s/solve", "h2d_bytes_per_step": 2 * N * bytes_field,
                 "d2h_bytes_per_step": N * bytes_field},
         "gpu_launches": int(launches),
+        "launches_before_timed": int(launches_before),
         "kernel_ms": kernel_ms,
         "clocks": clk.summary(),
         "link_build_s": t_links,

@@ -30,7 +30,7 @@ __global__ void __launch_bounds__(256) k_site(const Op op, const Fin fin, const 
   }
   if (NSUM == 0) return;
   __shared__ double smem[(256 / 32) * NS];
-  __shared__ double tot[BLAS_MAXSRC * NS];
+  __shared__ double tot[2 * BLAS_MAXSRC * NS];  // gridDim.y <= 2 * BLAS_MAXSRC
   __shared__ double scratch[32];
   __shared__ bool am_last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;

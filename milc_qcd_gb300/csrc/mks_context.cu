@@ -46,6 +46,19 @@ static const int EV_POOL = 4096;
 
 void timing_begin(int family) {
   Context &c = g_ctx;
+  if (c.capture) {
+    Capture &k = *c.capture;
+    k.family.push_back(family);
+    if (k.timed) {
+      cudaEvent_t e0, e1;
+      cudaEventCreate(&e0);
+      cudaEventCreate(&e1);
+      k.ev.push_back(e0);
+      k.ev.push_back(e1);
+      cudaEventRecord(e0, c.stream);
+    }
+    return;
+  }
   c.launches++;
   c.kernel_launches[family]++;
   if (!c.timing) return;
@@ -57,6 +70,10 @@ void timing_begin(int family) {
 void timing_end(int family) {
   Context &c = g_ctx;
   (void)family;
+  if (c.capture) {
+    if (c.capture->timed) cudaEventRecord(c.capture->ev.back(), c.stream);
+    return;
+  }
   if (!c.timing) return;
   cudaEventRecord(c.ev_pool[2 * c.ev_used + 1], c.stream);
   c.ev_used++;
@@ -73,6 +90,19 @@ int timing_flush() {
   }
   c.ev_used = 0;
   return MKS_OK;
+}
+
+void capture_account(const Capture &k) {
+  Context &c = g_ctx;
+  for (size_t i = 0; i < k.family.size(); i++) {
+    c.launches++;
+    c.kernel_launches[k.family[i]]++;
+    if (k.timed && c.timing) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, k.ev[2 * i], k.ev[2 * i + 1]);
+      c.kernel_ms[k.family[i]] += ms;
+    }
+  }
 }
 
 int ensure_red(int nsum, int blocks) {

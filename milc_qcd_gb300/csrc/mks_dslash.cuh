@@ -45,6 +45,20 @@ template <typename R> struct EpiLoad;
 template <> struct EpiLoad<double> { typedef VecF64 type; };
 template <> struct EpiLoad<float> { typedef VecF32 type; };
 
+// links of a scaled (FP16) type are used unscaled and their global scale
+// multiplies the neighbour vector instead: one multiply per vector component
+// rather than one per link entry
+template <class LinkT>
+__device__ __forceinline__ auto load_link(const LinkT &l, int par, int dir, int h, int Vh) {
+  if constexpr (LinkT::scaled) return l.load_raw(par, dir, h, Vh);
+  else return l.load(par, dir, h, Vh);
+}
+template <class LinkT, class InT>
+__device__ __forceinline__ auto load_in(const InT &v, int h, int Vh, const LinkT &l) {
+  if constexpr (LinkT::scaled) return v.load_mul(h, Vh, l.scale);
+  else return v.load(h, Vh);
+}
+
 struct NoFinish {
   __device__ void operator()(const double *, int) const {}
 };
@@ -61,11 +75,11 @@ k_dslash(const LinkT fat, const LinkT lng, const DslashArgs<InT, OutT, typename 
   const int h = tid / G, grp = tid - h * G;
   const int Vh = g.Vh;
   const int par = a.out_par, opar = 1 - par;
-  double sums[NB][NSUM > 0 ? NSUM : 1];
+  R sums[NB][NSUM > 0 ? NSUM : 1];  // per-site dot products in the kernel's precision
 #pragma unroll
   for (int s = 0; s < NB; s++)
 #pragma unroll
-    for (int k = 0; k < (NSUM > 0 ? NSUM : 1); k++) sums[s][k] = 0.0;
+    for (int k = 0; k < (NSUM > 0 ? NSUM : 1); k++) sums[s][k] = R(0);
 
   if (h < Vh) {
     int x, y, z, t;
@@ -90,35 +104,35 @@ k_dslash(const LinkT fat, const LinkT lng, const DslashArgs<InT, OutT, typename 
       const int hf3 = cb_index(g, cf3[0], cf3[1], cf3[2], cf3[3]);
       const int hb3 = cb_index(g, cb3[0], cb3[1], cb3[2], cb3[3]);
       {
-        const M3<R> U = fat.load(par, mu, h, Vh);
+        const M3<R> U = load_link(fat, par, mu, h, Vh);
 #pragma unroll
         for (int s = 0; s < NB; s++) {
           const int S = grp * NB + s;
-          if (S < a.nsrc) mv_acc(U, a.in[S].load(hf1, Vh), acc[s]);
+          if (S < a.nsrc) mv_acc(U, load_in<LinkT>(a.in[S], hf1, Vh, fat), acc[s]);
         }
       }
       {
-        const M3<R> U = lng.load(par, mu, h, Vh);
+        const M3<R> U = load_link(lng, par, mu, h, Vh);
 #pragma unroll
         for (int s = 0; s < NB; s++) {
           const int S = grp * NB + s;
-          if (S < a.nsrc) mv_acc(U, a.in[S].load(hf3, Vh), acc[s]);
+          if (S < a.nsrc) mv_acc(U, load_in<LinkT>(a.in[S], hf3, Vh, lng), acc[s]);
         }
       }
       {
-        const M3<R> U = fat.load(opar, mu, hb1, Vh);
+        const M3<R> U = load_link(fat, opar, mu, hb1, Vh);
 #pragma unroll
         for (int s = 0; s < NB; s++) {
           const int S = grp * NB + s;
-          if (S < a.nsrc) amv_sub(U, a.in[S].load(hb1, Vh), acc[s]);
+          if (S < a.nsrc) amv_sub(U, load_in<LinkT>(a.in[S], hb1, Vh, fat), acc[s]);
         }
       }
       {
-        const M3<R> U = lng.load(opar, mu, hb3, Vh);
+        const M3<R> U = load_link(lng, opar, mu, hb3, Vh);
 #pragma unroll
         for (int s = 0; s < NB; s++) {
           const int S = grp * NB + s;
-          if (S < a.nsrc) amv_sub(U, a.in[S].load(hb3, Vh), acc[s]);
+          if (S < a.nsrc) amv_sub(U, load_in<LinkT>(a.in[S], hb3, Vh, lng), acc[s]);
         }
       }
     }
@@ -135,18 +149,18 @@ k_dslash(const LinkT fat, const LinkT lng, const DslashArgs<InT, OutT, typename 
           acc[s].c[c].im = fma(cf, p.c[c].im, acc[s].c[c].im);
         }
         if (NSUM >= 1) {
-          double d = 0;
+          R d = 0;
 #pragma unroll
-          for (int c = 0; c < 3; c++) d += (double)p.c[c].re * acc[s].c[c].re + (double)p.c[c].im * acc[s].c[c].im;
+          for (int c = 0; c < 3; c++) d += p.c[c].re * acc[s].c[c].re + p.c[c].im * acc[s].c[c].im;
           sums[s][0] = d;
         }
         if (NSUM >= 3) {
           const V3<R> r = a.r[S].load(h, Vh);
-          double d1 = 0, d2 = 0;
+          R d1 = 0, d2 = 0;
 #pragma unroll
           for (int c = 0; c < 3; c++) {
-            d1 += (double)acc[s].c[c].re * r.c[c].re + (double)acc[s].c[c].im * r.c[c].im;
-            d2 += (double)acc[s].c[c].re * acc[s].c[c].re + (double)acc[s].c[c].im * acc[s].c[c].im;
+            d1 += acc[s].c[c].re * r.c[c].re + acc[s].c[c].im * r.c[c].im;
+            d2 += acc[s].c[c].re * acc[s].c[c].re + acc[s].c[c].im * acc[s].c[c].im;
           }
           sums[s][1] = d1;
           sums[s][2] = d2;
@@ -159,7 +173,7 @@ k_dslash(const LinkT fat, const LinkT lng, const DslashArgs<InT, OutT, typename 
     __shared__ double smem[(256 / 32 + 1) * MAXSRC * 3];
     __shared__ double tot[MAXSRC * 3];
     __shared__ double scratch[32];
-    block_reduce_grouped<NB, (NSUM > 0 ? NSUM : 1)>(sums, G, smem);
+    block_reduce_grouped<R, NB, (NSUM > 0 ? NSUM : 1)>(sums, G, smem);
     const int nslots = G * NB;
     const double *btot = smem + (blockDim.x >> 5) * nslots * NSUM;
     if (grid_reduce_last(btot, nslots * NSUM, a.partials, a.count, tot, scratch)) {

@@ -145,6 +145,12 @@ struct VecF32 {
 #pragma unroll
     for (int c = 0; c < 3; c++) p[(size_t)c * Vh + h] = make_float2(v.c[c].re, v.c[c].im);
   }
+  __device__ __forceinline__ V3<float> load_mul(int h, int Vh, float f) const {
+    V3<float> v = load(h, Vh);
+#pragma unroll
+    for (int c = 0; c < 3; c++) { v.c[c].re *= f; v.c[c].im *= f; }
+    return v;
+  }
 };
 struct VecF16 {
   __half2 *p;   // [3][Vh]
@@ -152,6 +158,16 @@ struct VecF16 {
   __device__ __forceinline__ V3<float> load(int h, int Vh) const {
     V3<float> v;
     float s = __ldg(norm + h);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      float2 a = __half22float2(__ldg(p + (size_t)c * Vh + h));
+      v.c[c] = {a.x * s, a.y * s};
+    }
+    return v;
+  }
+  __device__ __forceinline__ V3<float> load_mul(int h, int Vh, float f) const {
+    V3<float> v;
+    float s = __ldg(norm + h) * f;
 #pragma unroll
     for (int c = 0; c < 3; c++) {
       float2 a = __half22float2(__ldg(p + (size_t)c * Vh + h));
@@ -171,6 +187,7 @@ struct VecF16 {
 };
 
 struct LinkF64 {
+  static constexpr bool scaled = false;
   const double2 *p;  // [par][dir][9][Vh]
   __device__ __forceinline__ M3<double> load(int par, int dir, int h, int Vh) const {
     const double2 *b = p + ((size_t)(par * 4 + dir) * 9) * Vh + h;
@@ -181,6 +198,7 @@ struct LinkF64 {
   }
 };
 struct LinkF32 {
+  static constexpr bool scaled = false;
   const float4 *a;  // [par][dir][4][Vh]
   const float2 *b;  // [par][dir][Vh]
   __device__ __forceinline__ M3<float> load(int par, int dir, int h, int Vh) const {
@@ -198,9 +216,30 @@ struct LinkF32 {
   }
 };
 struct LinkF16 {
+  static constexpr bool scaled = true;  // entries are stored divided by `scale`
   const uint4 *a;     // [par][dir][2][Vh]: entries 0..7 as 16 halves
   const __half2 *b;   // [par][dir][Vh]: entry 8
   float scale;
+  // unscaled entries: U = scale * load_raw(); D_eo folds `scale` into the vector
+  __device__ __forceinline__ M3<float> load_raw(int par, int dir, int h, int Vh) const {
+    const uint4 *pa = a + ((size_t)(par * 4 + dir) * 2) * Vh + h;
+    M3<float> m;
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+      uint4 q = __ldg(pa + (size_t)k * Vh);
+      unsigned w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        __half2 hv = *reinterpret_cast<__half2 *>(&w[j]);
+        float2 f = __half22float2(hv);
+        int e = 4 * k + j;
+        m.e[e / 3][e % 3] = {f.x, f.y};
+      }
+    }
+    float2 f = __half22float2(__ldg(b + (size_t)(par * 4 + dir) * Vh + h));
+    m.e[2][2] = {f.x, f.y};
+    return m;
+  }
   __device__ __forceinline__ M3<float> load(int par, int dir, int h, int Vh) const {
     const uint4 *pa = a + ((size_t)(par * 4 + dir) * 2) * Vh + h;
     M3<float> m;
@@ -263,10 +302,23 @@ struct Context {
   std::vector<cudaEvent_t> ev_pool;
   std::vector<int> ev_family;  // family per pair
   int ev_used = 0;
+  // CUDA-graph capture of solver iterations: while `capture` is set,
+  // launches are recorded into it instead of the event pool
+  struct Capture *capture = nullptr;
 };
 
 Context &ctx();
 int check_ready(bool need_lattice = true);
+
+// A captured batch of launches: per kernel node its family and (when the
+// batch was captured with timing on) its own event pair, so each replay of
+// the graph can be timed and counted like eager launches.
+struct Capture {
+  std::vector<int> family;
+  std::vector<cudaEvent_t> ev;  // 2 per node when timed
+  bool timed = false;
+};
+void capture_account(const Capture &cap);  // after a replay has completed
 
 // timed launch helpers
 void timing_begin(int family);

@@ -16,15 +16,19 @@ namespace mks {
 // belong to slot (t % G)*NB + s for s < NB.  Result: tot[slot*NSUM + k] in
 // shared memory on return (valid after the trailing __syncthreads), for
 // slots < nslots = G*NB.  smem must hold (blockDim/32) * G*NB*NSUM doubles.
-template <int NB, int NSUM>
-__device__ __forceinline__ void block_reduce_grouped(double (&v)[NB][NSUM], int G, double *smem) {
+// The per-thread values and the warp-level shuffles use T (float in the
+// sloppy solvers: GB300 runs FP64 at a small fraction of the FP32 rate, so
+// per-site products and the first 32-way sums stay in FP32); from the warp
+// totals on, everything is FP64.
+template <typename T, int NB, int NSUM>
+__device__ __forceinline__ void block_reduce_grouped(T (&v)[NB][NSUM], int G, double *smem) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int nslots = G * NB;
 #pragma unroll
   for (int s = 0; s < NB; s++)
 #pragma unroll
     for (int k = 0; k < NSUM; k++) {
-      double x = v[s][k];
+      T x = v[s][k];
       for (int o = 16; o >= G; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
       v[s][k] = x;
     }
@@ -32,7 +36,7 @@ __device__ __forceinline__ void block_reduce_grouped(double (&v)[NB][NSUM], int 
 #pragma unroll
     for (int s = 0; s < NB; s++)
 #pragma unroll
-      for (int k = 0; k < NSUM; k++) smem[(warp * nslots + lane * NB + s) * NSUM + k] = v[s][k];
+      for (int k = 0; k < NSUM; k++) smem[(warp * nslots + lane * NB + s) * NSUM + k] = (double)v[s][k];
   }
   __syncthreads();
   // sum over warps, in warp order

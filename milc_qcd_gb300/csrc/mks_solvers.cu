@@ -42,7 +42,10 @@ static int ws(const std::string &name, size_t bytes, void **out) {
   return MKS_OK;
 }
 
+void graphs_free_all();
+
 void ws_free_all() {
+  graphs_free_all();
   for (auto &kv : g_ws) dev_free(kv.second.p);
   g_ws.clear();
 }
@@ -150,7 +153,7 @@ struct PtrSet16 { __half2 *p[BLAS_MAXSRC]; float *n[BLAS_MAXSRC]; };
 
 // |v|^2
 template <typename T2> struct OpNorm {
-  T2 *v[BLAS_MAXSRC];
+  T2 *v[2 * BLAS_MAXSRC];
   int Vh;
   __device__ void operator()(int h, int s, double *out) const {
     double a = 0;
@@ -166,18 +169,21 @@ template <typename T2> struct OpNorm {
 // CG restart / reliable update residual (FP64):
 //   ttt <- ttt - 4m^2 x ; r <- src + ttt ; sum |r|^2, and the relative residual
 //   sum |r|^2/|x|^2 (d_congrad5_fn_milc.c:196-216).  Optionally p <- r.
+// Entry s of the op works on source map[s]; when tzero[s] is set the
+// source's x is known to be zero and D D x is not computed (ttt taken as 0).
 struct OpResid64 {
   double2 *ttt[BLAS_MAXSRC], *x[BLAS_MAXSRC], *src[BLAS_MAXSRC], *r[BLAS_MAXSRC], *p[BLAS_MAXSRC];
   const CgState *st;
   double msq4[BLAS_MAXSRC];
+  int map[BLAS_MAXSRC], tzero[BLAS_MAXSRC];
   int Vh, setp;
   __device__ void operator()(int h, int s, double *out) const {
-    if (st && st[s].status != ST_HOST) { out[0] = 0; out[1] = 0; return; }
+    if (st && st[map[s]].status != ST_HOST) { out[0] = 0; out[1] = 0; return; }
     double a = 0, xx = 0;
 #pragma unroll
     for (int c = 0; c < 3; c++) {
       size_t i = (size_t)c * Vh + h;
-      double2 t = ttt[s][i], xv = x[s][i], sv = src[s][i];
+      double2 t = tzero[s] ? make_double2(0.0, 0.0) : ttt[s][i], xv = x[s][i], sv = src[s][i];
       double2 rv = make_double2(sv.x + (t.x + (-msq4[s]) * xv.x), sv.y + (t.y + (-msq4[s]) * xv.y));
       r[s][i] = rv;
       if (setp) p[s][i] = rv;
@@ -192,10 +198,11 @@ struct OpResid64 {
 struct FinResid {
   CgState *st;
   int *skip;
+  int map[BLAS_MAXSRC];
   __device__ void operator()(const double *t, int nsrc) const {
     int s = threadIdx.x;
     if (s < nsrc) {
-      CgState &c = st[s];
+      CgState &c = st[map[s]];
       if (c.status == ST_HOST) {
         c.rsq = t[2 * s];
         c.actual_rsq = t[2 * s];
@@ -220,7 +227,7 @@ template <typename R> struct OpUpdate {
     const CgState &c = st[s];
     if (c.status != ST_RUN) { out[0] = 0; if (relres) out[1] = 0; return; }
     const R a = (R)c.a, b = (R)c.b;
-    double rr = 0, xx = 0;
+    R rr = 0, xx = 0;  // per-site sums in the storage precision (FP64 is slow on GB300)
     V3<R> pn;
 #pragma unroll
     for (int k = 0; k < 3; k++) {
@@ -228,8 +235,8 @@ template <typename R> struct OpUpdate {
       T2 xv = x[s][i], pv = p[s][i], rv = r[s][i], tv = ttt[s][i];
       xv.x = xv.x + a * pv.x; xv.y = xv.y + a * pv.y;
       rv.x = rv.x + a * tv.x; rv.y = rv.y + a * tv.y;
-      rr += (double)rv.x * rv.x + (double)rv.y * rv.y;
-      xx += (double)xv.x * xv.x + (double)xv.y * xv.y;
+      rr += rv.x * rv.x + rv.y * rv.y;
+      xx += xv.x * xv.x + xv.y * xv.y;
       pv.x = rv.x + b * pv.x; pv.y = rv.y + b * pv.y;
       x[s][i] = xv; r[s][i] = rv; p[s][i] = pv;
       pn.c[k] = {(R)pv.x, (R)pv.y};
@@ -465,6 +472,29 @@ static int tune_shape(const LinkT &fat, const LinkT &lng, int nsrc, Shape *best)
   return MKS_OK;
 }
 
+// MKS_SHAPE="prec:nsrc:G:NB:block[,...]" fixes shapes by hand (a tuning
+// cache written by the user); entries must satisfy G*NB >= nsrc, G*NB <= 16,
+// NB in {1,2,4,8}, G a power of two, block in {128,256}.
+static bool shape_override(int prec, int nsrc, Shape *out) {
+  const char *e = getenv("MKS_SHAPE");
+  if (!e) return false;
+  std::string str(e);
+  size_t pos = 0;
+  while (pos < str.size()) {
+    size_t end = str.find(',', pos);
+    if (end == std::string::npos) end = str.size();
+    int p, n, G, NB, B;
+    if (sscanf(str.substr(pos, end - pos).c_str(), "%d:%d:%d:%d:%d", &p, &n, &G, &NB, &B) == 5 && p == prec &&
+        n == nsrc && G >= 1 && G <= 16 && (G & (G - 1)) == 0 && (NB == 1 || NB == 2 || NB == 4 || NB == 8) &&
+        G * NB >= nsrc && G * NB <= MAXSRC && (B == 128 || B == 256)) {
+      *out = {G, NB, B};
+      return true;
+    }
+    pos = end + 1;
+  }
+  return false;
+}
+
 template <typename R, class LinkT, class InT, class OutT, int EPI, int NSUM, class Fin>
 static int launch_dslash(int family, const LinkT &fat, const LinkT &lng,
                          DslashArgs<InT, OutT, typename EpiLoad<R>::type> &a, const Fin &fin) {
@@ -472,7 +502,7 @@ static int launch_dslash(int family, const LinkT &fat, const LinkT &lng,
   Shape &sh = g_shape[pk][a.nsrc];
   if (sh.G == 0) {
     Shape t;
-    MKS_TRY(tune_shape(fat, lng, a.nsrc, &t));
+    if (!shape_override(pk, a.nsrc, &t)) MKS_TRY(tune_shape(fat, lng, a.nsrc, &t));
     sh = t;
   }
   if (a.nsrc > 1 && family != MKS_K_DSLASH_F64) family = MKS_K_DSLASH_MRHS;
@@ -705,23 +735,154 @@ static int cg_iteration(const LinkSlot &sl, int par, int nsrc, int prec, const d
 
 // FP64 true residual for sources with status ST_HOST: r = src - M^dag M x,
 // |r|^2 -> state (rsq, actual_rsq, final_rsq, iter++).  setp: p <- r.
+// ------------------------------------------------------------------
+// CUDA graphs for the solver iterations.  A batch of poll_interval()
+// iterations (3 launches each) is captured once per configuration and then
+// replayed with one cudaGraphLaunch; the first batch of a configuration runs
+// eagerly so that the autotuner and the scratch buffers are settled before
+// capture.  The key holds every pointer and scalar the launches bake in.
+struct GraphEntry {
+  std::vector<uint64_t> key;
+  int seen = 0;
+  cudaGraphExec_t exec = nullptr;
+  Capture cap;
+};
+static std::vector<GraphEntry> g_graphs;
+
+static bool graphs_enabled() {
+  static int v = -1;
+  if (v < 0) {
+    const char *e = getenv("MKS_GRAPH");
+    v = e ? atoi(e) : 1;
+  }
+  return v != 0;
+}
+
+static void free_graph(GraphEntry &e) {
+  if (e.exec) cudaGraphExecDestroy(e.exec);
+  for (auto ev : e.cap.ev) cudaEventDestroy(ev);
+  e.exec = nullptr;
+  e.cap = Capture();
+}
+
+void graphs_free_all() {
+  for (auto &e : g_graphs) free_graph(e);
+  g_graphs.clear();
+}
+
+template <typename T> static void key_push(std::vector<uint64_t> &k, const T &v) {
+  uint64_t u = 0;
+  memcpy(&u, &v, sizeof(T) < 8 ? sizeof(T) : 8);
+  k.push_back(u);
+}
+
+static int cg_iteration(const LinkSlot &sl, int par, int nsrc, int prec, const double *msq4, CgFields &f, Solver &S);
+
+static int run_batch(const LinkSlot &sl, int par, int nsrc, int prec, const double *msq4, CgFields &f, Solver &S,
+                     int np) {
+  Context &c = ctx();
+  if (!graphs_enabled()) {
+    for (int k = 0; k < np; k++) MKS_TRY(cg_iteration(sl, par, nsrc, prec, msq4, f, S));
+    return MKS_OK;
+  }
+  std::vector<uint64_t> key;
+  key_push(key, nsrc); key_push(key, prec); key_push(key, par); key_push(key, np); key_push(key, (int)c.timing);
+  key_push(key, c.geom.Vh); key_push(key, c.geom.nx); key_push(key, c.geom.ny); key_push(key, c.geom.nz);
+  key_push(key, c.geom.nt);
+  key_push(key, sl.fat64); key_push(key, sl.lng64); key_push(key, sl.fat32a); key_push(key, sl.lng32a);
+  key_push(key, sl.fat32b); key_push(key, sl.lng32b); key_push(key, sl.fat16a); key_push(key, sl.lng16a);
+  key_push(key, sl.fat16b); key_push(key, sl.lng16b); key_push(key, sl.fat16scale); key_push(key, sl.lng16scale);
+  key_push(key, S.st); key_push(key, S.skip); key_push(key, c.red.partials); key_push(key, c.red.count);
+  for (int s = 0; s < nsrc; s++) {
+    key_push(key, msq4[s]);
+    key_push(key, f.x[s]); key_push(key, f.p[s]); key_push(key, f.r[s]); key_push(key, f.ttt[s]); key_push(key, f.t[s]);
+    key_push(key, f.x32[s]); key_push(key, f.p32[s]); key_push(key, f.r32[s]); key_push(key, f.ttt32[s]);
+    key_push(key, f.t32[s]); key_push(key, f.p16[s]); key_push(key, f.t16[s]); key_push(key, f.p16n[s]);
+    key_push(key, f.t16n[s]);
+  }
+  GraphEntry *e = nullptr;
+  for (auto &g : g_graphs)
+    if (g.key == key) { e = &g; break; }
+  if (!e) {
+    if (g_graphs.size() >= 8) { free_graph(g_graphs.front()); g_graphs.erase(g_graphs.begin()); }
+    g_graphs.emplace_back();
+    e = &g_graphs.back();
+    e->key = key;
+  }
+  if (!e->exec) {
+    if (e->seen++ == 0) {
+      for (int k = 0; k < np; k++) MKS_TRY(cg_iteration(sl, par, nsrc, prec, msq4, f, S));
+      return MKS_OK;
+    }
+    Capture cap;
+    cap.timed = c.timing;
+    c.capture = &cap;
+    int rc = MKS_OK;
+    cudaError_t e0 = cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeRelaxed);
+    if (e0 == cudaSuccess)
+      for (int k = 0; k < np && rc >= 0; k++) rc = cg_iteration(sl, par, nsrc, prec, msq4, f, S);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e1 = e0 == cudaSuccess ? cudaStreamEndCapture(c.stream, &graph) : e0;
+    c.capture = nullptr;
+    if (rc < 0 || e1 != cudaSuccess || !graph) {
+      if (graph) cudaGraphDestroy(graph);
+      for (auto ev : cap.ev) cudaEventDestroy(ev);
+      cudaGetLastError();
+      if (rc < 0) return rc;
+      set_last_error(e1, "cudaStreamEndCapture", __FILE__, __LINE__);
+      return MKS_ERR_CUDA;
+    }
+    cudaError_t e2 = cudaGraphInstantiate(&e->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e2 != cudaSuccess) {
+      for (auto ev : cap.ev) cudaEventDestroy(ev);
+      e->exec = nullptr;
+      set_last_error(e2, "cudaGraphInstantiate", __FILE__, __LINE__);
+      return MKS_ERR_CUDA;
+    }
+    e->cap = cap;
+  }
+  MKS_CUDA(cudaGraphLaunch(e->exec, c.stream));
+  MKS_CUDA(cudaStreamSynchronize(c.stream));
+  capture_account(e->cap);
+  return MKS_OK;
+}
+
+// FP64 true residual r = src - (sigma - D D) x for the sources flagged
+// (need[s]); xzero[s] marks sources whose x is exactly zero (D D x skipped).
 static int true_residual(const LinkSlot &sl, int par, int nsrc, const double *msq4, CgFields &f, Solver &S, int setp,
-                         std::vector<double> *relrsq) {
-  MKS_TRY(apply_DD64(sl, par, nsrc, f.x, f.t, f.ttt));
+                         const std::vector<int> &need, const std::vector<int> &xzero, std::vector<double> *relrsq) {
+  int idx[MAXSRC], nd = 0, ndd = 0;
+  double2 *xs[MAXSRC], *ts[MAXSRC], *tts[MAXSRC];
+  for (int s = 0; s < nsrc; s++) {
+    if (!need[s]) continue;
+    idx[nd++] = s;
+    if (!xzero[s]) { xs[ndd] = f.x[s]; ts[ndd] = f.t[s]; tts[ndd] = f.ttt[s]; ndd++; }
+  }
+  if (nd == 0) return MKS_OK;
+  if (ndd > 0) MKS_TRY(apply_DD64(sl, par, ndd, xs, ts, tts));
   OpResid64 op;
   memset(&op, 0, sizeof op);
-  for (int s = 0; s < nsrc; s++) { op.ttt[s] = f.ttt[s]; op.x[s] = f.x[s]; op.src[s] = f.src[s]; op.r[s] = f.r[s]; op.p[s] = f.p[s]; }
-  op.st = S.st; for (int s = 0; s < nsrc; s++) op.msq4[s] = msq4[s]; op.Vh = (int)ctx().Vh; op.setp = setp;
+  FinResid fin;
+  memset(&fin, 0, sizeof fin);
+  for (int k = 0; k < nd; k++) {
+    int s = idx[k];
+    op.ttt[k] = f.ttt[s]; op.x[k] = f.x[s]; op.src[k] = f.src[s]; op.r[k] = f.r[s]; op.p[k] = f.p[s];
+    op.msq4[k] = msq4[s]; op.map[k] = s; op.tzero[k] = xzero[s];
+    fin.map[k] = s;
+  }
+  op.st = S.st; op.Vh = (int)ctx().Vh; op.setp = setp;
+  fin.st = S.st; fin.skip = S.skip;
   double *tot;
   MKS_TRY(wsv("cg_tot2", 2 * MAXSRC, &tot));
-  MKS_TRY((launch_site<OpResid64, 2, FinResid>(MKS_K_BLAS, op, FinResid{S.st, S.skip}, nullptr, nsrc, tot)));
+  MKS_TRY((launch_site<OpResid64, 2, FinResid>(MKS_K_BLAS, op, fin, nullptr, nd, tot)));
   if (relrsq) {
-    std::vector<double> h(2 * nsrc);
+    std::vector<double> h(2 * nd);
     Context &c = ctx();
-    MKS_CUDA(cudaMemcpyAsync(h.data(), tot, 2 * nsrc * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    MKS_CUDA(cudaMemcpyAsync(h.data(), tot, 2 * nd * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     MKS_CUDA(cudaStreamSynchronize(c.stream));
-    relrsq->resize(nsrc);
-    for (int s = 0; s < nsrc; s++) (*relrsq)[s] = sqrt(2.0 * h[2 * s + 1] / (double)c.V);
+    relrsq->assign(nsrc, 0.0);
+    for (int k = 0; k < nd; k++) (*relrsq)[idx[k]] = sqrt(2.0 * h[2 * k + 1] / (double)c.V);
   }
   return MKS_OK;
 }
@@ -749,18 +910,20 @@ static int block_cg_shifted(int slot, int par, int nsrc, const double *msq4, con
   MKS_TRY(wsv("cg_state", MAXSRC, &S.st));
   MKS_TRY(wsv("cg_skip", 1, &S.skip));
 
-  // source norms
+  // source norms and initial-guess norms (a zero guess needs no D D x)
+  std::vector<int> xzero(nsrc, 0);
   {
     OpNorm<double2> op;
     memset(&op, 0, sizeof op);
-    for (int s = 0; s < nsrc; s++) op.v[s] = f.src[s];
+    for (int s = 0; s < nsrc; s++) { op.v[s] = f.src[s]; op.v[nsrc + s] = f.x[s]; }
     op.Vh = (int)c.Vh;
     double *tot;
-    MKS_TRY(wsv("cg_tot1", MAXSRC, &tot));
-    MKS_TRY((launch_site<OpNorm<double2>, 1, FinNone>(MKS_K_BLAS, op, FinNone(), nullptr, nsrc, tot)));
-    std::vector<double> h(nsrc);
-    MKS_CUDA(cudaMemcpyAsync(h.data(), tot, nsrc * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    MKS_TRY(wsv("cg_tot1", 2 * MAXSRC, &tot));
+    MKS_TRY((launch_site<OpNorm<double2>, 1, FinNone>(MKS_K_BLAS, op, FinNone(), nullptr, 2 * nsrc, tot)));
+    std::vector<double> h(2 * nsrc);
+    MKS_CUDA(cudaMemcpyAsync(h.data(), tot, 2 * nsrc * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     MKS_CUDA(cudaStreamSynchronize(c.stream));
+    for (int s = 0; s < nsrc; s++) xzero[s] = h[nsrc + s] == 0.0;
     std::vector<CgState> hs(nsrc);
     memset(hs.data(), 0, nsrc * sizeof(CgState));
     for (int s = 0; s < nsrc; s++) {
@@ -808,8 +971,10 @@ static int block_cg_shifted(int slot, int par, int nsrc, const double *msq4, con
         MKS_TRY((launch_site<OpAccumX, 0, FinNone>(MKS_K_BLAS, ax, FinNone(), nullptr, nsrc)));
       }
       std::vector<double> relrsq;
-      MKS_TRY(true_residual(sl, par, nsrc, msq4, f, S, mixed ? (first ? 1 : 0) : 1,
-                            arg->relresid > 0 ? &relrsq : nullptr));
+      std::vector<int> need(nsrc);
+      for (int s = 0; s < nsrc; s++) need[s] = hs[s].status == ST_HOST;
+      MKS_TRY(true_residual(sl, par, nsrc, msq4, f, S, mixed ? (first ? 1 : 0) : 1, need,
+                            first ? xzero : std::vector<int>(nsrc, 0), arg->relresid > 0 ? &relrsq : nullptr));
       if (mixed) {
         OpDemote dm;
         memset(&dm, 0, sizeof dm);
@@ -852,7 +1017,7 @@ static int block_cg_shifted(int slot, int par, int nsrc, const double *msq4, con
     }
     if (!any_run) break;
     int np = poll_interval();
-    for (int k = 0; k < np; k++) MKS_TRY(cg_iteration(sl, par, nsrc, prec, msq4, f, S));
+    MKS_TRY(run_batch(sl, par, nsrc, prec, msq4, f, S, np));
     if (++guard > 10000000) return MKS_ERR_TIMEOUT;
   }
   if (mixed) {
@@ -1297,7 +1462,7 @@ template <typename R> struct OpShiftUpdate {
     const int n = m.num_now, jl = m.j_low;
     const R bl = (R)m.beta_i[jl];
     T2 rn[3];
-    double rr = 0;
+    R rr = 0;  // per-site sum in the storage precision
 #pragma unroll
     for (int k = 0; k < 3; k++) {
       size_t i = (size_t)k * Vh + h;
@@ -1305,7 +1470,7 @@ template <typename R> struct OpShiftUpdate {
       rv.x = rv.x + bl * tv.x; rv.y = rv.y + bl * tv.y;
       rn[k] = rv;
       r[i] = rv;
-      rr += (double)rv.x * rv.x + (double)rv.y * rv.y;
+      rr += rv.x * rv.x + rv.y * rv.y;
     }
     for (int j = 0; j < n; j++) {
       const R bj = (R)m.beta_i[j], zj = (R)m.zeta_ip1[j], aj = (R)m.alpha[j];
