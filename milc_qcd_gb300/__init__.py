@@ -31,7 +31,7 @@ from ._lib import (MKS_EVEN as EVEN, MKS_ODD as ODD, MKS_EVENANDODD as EVENANDOD
 __all__ = ["EVEN", "ODD", "EVENANDODD", "PREC_HALF", "PREC_SINGLE", "PREC_DOUBLE", "QuarkInvertControl",
            "init", "set_lattice", "load_fn_links", "get_fn_links", "dslash_fn_field", "ks_congrad_parity",
            "ks_congrad_block_parity", "mat_invert_uml_field", "mat_invert_block_uml",
-           "ks_multicg_offset_field", "load_hisq_links", "load_asqtad_links", "get_hisq_aux",
+           "ks_multicg_offset_field", "ks_ratinv", "ks_rateval", "load_hisq_links", "load_asqtad_links", "get_hisq_aux",
            "eo_fermion_force_multi", "gen_thin_links", "apply_phases", "gen_vector", "gen_momenta",
            "MksError"]
 
@@ -153,6 +153,28 @@ def ks_multicg_offset_field(src, psim, offsets, qic, fn=0):
                "mks_ks_multicg_offset_field")
     qic.take(res[0])
     return it, [QuarkInvertControl().take(res[i]) for i in range(n)]
+
+
+def ks_ratinv(src, roots, residues, qic, fn=0):
+    """Rational-function inversion, ks_imp_rhmc/ks_ratinv.c:29-112: one
+    multi-shift solve with offsets roots[1..order] (roots[0] is the constant
+    term's slot).  Returns (iterations, psim list)."""
+    order = len(roots) - 1
+    psim = [np.zeros_like(src) for _ in range(order)]
+    it, _ = ks_multicg_offset_field(src, psim, np.asarray(roots[1:], dtype=np.float64), qic, fn)
+    return it, psim
+
+
+def ks_rateval(src, psim, residues, parity):
+    """dest = residues[0] src + sum_j residues[j+1] psim[j] on `parity`
+    (ks_imp_rhmc/ks_ratinv.c:116-137); other sites are zero."""
+    V = src.shape[0]
+    lo, hi = (0, V // 2) if parity == EVEN else ((V // 2, V) if parity == ODD else (0, V))
+    dest = np.zeros_like(src)
+    dest[lo:hi] = residues[0] * src[lo:hi]
+    for j, p in enumerate(psim):
+        dest[lo:hi] += residues[j + 1] * p[lo:hi]
+    return dest
 
 
 def load_hisq_links(thin_phased, eps_naik=(0.0,)):

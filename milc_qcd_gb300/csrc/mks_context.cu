@@ -55,7 +55,8 @@ void timing_begin(int family) {
       cudaEventCreate(&e1);
       k.ev.push_back(e0);
       k.ev.push_back(e1);
-      cudaEventRecord(e0, c.stream);
+      // an external record becomes an event-record node that fires on every replay
+      cudaEventRecordWithFlags(e0, c.stream, cudaEventRecordExternal);
     }
     return;
   }
@@ -71,7 +72,7 @@ void timing_end(int family) {
   Context &c = g_ctx;
   (void)family;
   if (c.capture) {
-    if (c.capture->timed) cudaEventRecord(c.capture->ev.back(), c.stream);
+    if (c.capture->timed) cudaEventRecordWithFlags(c.capture->ev.back(), c.stream, cudaEventRecordExternal);
     return;
   }
   if (!c.timing) return;

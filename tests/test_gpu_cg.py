@@ -94,3 +94,29 @@ def test_mat_invert_uml_matches_oracle(gpu, oracle_cls, prec):
     # M x = src, checked with the oracle's D
     Mx = 2 * 0.05 * x + orc.dslash(fat, lng, x, m.EVENANDODD)
     assert rel(Mx, src) < 1e-9
+
+
+def test_graph_replay_with_kernel_timing(gpu, oracle_cls):
+    """Solver batches replay as CUDA graphs after their first (eager) run;
+    with kernel timing on, the replays carry their own event-record nodes and
+    are counted and timed like eager launches."""
+    import ctypes
+    m = gpu
+    orc, fat, lng = _setup(m, oracle_cls)
+    lib = m._lib.load()
+    b = m.gen_vector(DIMS, 91, m.EVEN)
+    qic = m.QuarkInvertControl(resid=1e-10, max=2000, nrestart=5, parity=m.EVEN, prec=m.PREC_SINGLE)
+    lib.mks_timing_reset()
+    lib.mks_timing_enable(1)
+    xs = []
+    for rep in range(3):
+        x = np.zeros_like(b)
+        m.ks_congrad_parity(b, x, qic, 0.02)
+        assert qic.converged == 1
+        xs.append(x)
+    t, n = ctypes.c_double(), ctypes.c_longlong()
+    m.check(lib.mks_timing_get(1, ctypes.byref(t), ctypes.byref(n)), "timing")
+    lib.mks_timing_enable(0)
+    assert n.value > 3 * 2 * 20 and t.value > 0
+    # replayed solves give the same answer as the eager first one
+    assert rel(xs[2], xs[0]) < 1e-12 and rel(xs[1], xs[0]) < 1e-12

@@ -56,3 +56,25 @@ def test_multishift_rejects_nonpositive_offset(gpu, oracle_cls):
     qic = m.QuarkInvertControl(resid=1e-8, parity=m.EVEN)
     with pytest.raises(m.MksError):
         m.ks_multicg_offset_field(b, [np.zeros_like(b)] * 2, [0.1, 0.0], qic)
+
+
+def test_ratinv_rateval_against_single_solves(gpu, oracle_cls):
+    """R(A) b = a0 b + sum_j a_j (A + sigma_j)^-1 b, A = -D_eo D_oe, through the
+    multi-shift solve (ks_ratinv) and the linear combination (ks_rateval)."""
+    m = gpu
+    U, orc, L = hisq_setup(m, oracle_cls, DIMS)
+    fat, lng = L["fat"][0], L["lng"][0]
+    m.set_lattice(DIMS)
+    m.load_fn_links(fat, lng)
+    b = m.gen_vector(DIMS, 54, m.EVEN)
+    roots = [0.0, 0.002, 0.03, 0.4]
+    residues = [0.7, 0.05, 0.2, 0.9]
+    qic = m.QuarkInvertControl(resid=1e-11, max=2000, nrestart=5, parity=m.EVEN, prec=m.PREC_DOUBLE)
+    it, psim = m.ks_ratinv(b, roots, residues, qic)
+    dest = m.ks_rateval(b, psim, residues, m.EVEN)
+    ref = residues[0] * b
+    for j, s in enumerate(roots[1:]):
+        _, x, _ = orc.congrad(fat, lng, b, np.zeros_like(b), np.sqrt(s) / 2, m.EVEN, 1e-13, 0.0, 2000, 5)
+        ref = ref + residues[j + 1] * x
+    V2 = b.shape[0] // 2
+    assert rel(dest[:V2], ref[:V2]) < 1e-9
