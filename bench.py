@@ -147,6 +147,70 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- extras
+def extras(m, lib, _lib, torch, srcs):
+    """Figures for the other workloads of the same family, measured after the
+    headline (not part of `value`): the multi-source sweep N = 1, 4, 8, 16
+    (32^3x64, FP32 inner solve), the 11-offset multi-shift solve (32^3x64,
+    sigma_i = 4m^2 + s_i, s_i log-uniform in [1e-4, 1]) in FP64 and mixed
+    precision, and the HISQ fermion force on 16^3x32 (6 terms)."""
+    out = {}
+    sweep = {}
+    for n in (1, 4, 8, 16):
+        ss = [srcs[k % len(srcs)] * (1.0 + 0.01 * k) for k in range(n)]
+        d_s = [torch.from_numpy(np.ascontiguousarray(s)).to("cuda") for s in ss]
+        d_x = [torch.zeros_like(t) for t in d_s]
+        arg = _lib.InvertArg(1000, 10, m.EVEN, m.PREC_SINGLE, RESID, 0.0, 0.1)
+        res = (_lib.InvertResult * n)()
+        VP = ctypes.c_void_p * n
+        for rep in range(2):  # first run tunes and captures
+            for t in d_x:
+                t.zero_()
+            torch.cuda.synchronize()
+            t0 = time.time()
+            m.check(lib.mks_ks_congrad_block_parity_dev(n, VP(*[t.data_ptr() for t in d_s]),
+                                                        VP(*[t.data_ptr() for t in d_x]), MASS, 0,
+                                                        ctypes.byref(arg), res), "sweep")
+            torch.cuda.synchronize()
+            dt = time.time() - t0
+        sweep[str(n)] = {"s_per_solve": dt / n, "converged": all(res[k].converged for k in range(n))}
+    out["multi_rhs_f32_s_per_solve"] = sweep
+    sig = 4 * MASS ** 2 + np.logspace(-4, 0, 11)
+    d_b = torch.from_numpy(srcs[0]).to("cuda")
+    d_p = [torch.zeros_like(d_b) for _ in sig]
+    VP = ctypes.c_void_p * len(sig)
+    ms = {}
+    for name, prec in (("f64", m.PREC_DOUBLE), ("single", m.PREC_SINGLE), ("half", m.PREC_HALF)):
+        arg = _lib.InvertArg(1000, 10, m.EVEN, prec, RESID, 0.0, 0.1)
+        res = (_lib.InvertResult * len(sig))()
+        for rep in range(2):
+            torch.cuda.synchronize()
+            t0 = time.time()
+            it = m.check(lib.mks_ks_multicg_offset_field_dev(d_b.data_ptr(), VP(*[t.data_ptr() for t in d_p]),
+                                                             sig.ctypes.data_as(_lib.DP), len(sig), 0,
+                                                             ctypes.byref(arg), res), "multishift")
+            torch.cuda.synchronize()
+            dt = time.time() - t0
+        ms[name] = {"s": dt, "iters": it, "max_final_rsq": max(res[k].final_rsq for k in range(len(sig))),
+                    "converged": all(res[k].converged for k in range(len(sig)))}
+    out["multishift_11_offsets"] = ms
+    fdims = (16, 16, 16, 32)
+    m.set_lattice(fdims)
+    U = m.apply_phases(fdims, m.gen_thin_links(fdims, 77, LINK_A))
+    m.load_hisq_links(U)
+    xxx = [m.gen_vector(fdims, 300 + j, m.EVENANDODD) for j in range(6)]
+    res6 = list(np.linspace(0.1, 1.0, 6))
+    mom = np.zeros((int(np.prod(fdims)), 4, 10))
+    m.eo_fermion_force_multi(0.01, res6, xxx, mom)
+    t0 = time.time()
+    m.eo_fermion_force_multi(0.01, res6, xxx, mom)
+    dt = time.time() - t0
+    out["hisq_force_16c32_6terms"] = {"s_per_call": dt, "gflops_fp64": lib.mks_force_flops_last() / dt / 1e9,
+                                      "includes": "host<->device copies of 6 vectors and the momenta"}
+    m.set_lattice(DIMS)
+    return out
+
+
 # ---------------------------------------------------------------- GPU arm
 def gpu_arm(args):
     import torch
@@ -300,6 +364,8 @@ def gpu_arm(args):
         "clocks": clk.summary(),
         "link_build_s": t_links,
     }
+    if not args.no_extras:
+        line["extras"] = extras(m, lib, _lib, torch, srcs)
     if not args.no_cpu and world == 1:
         base = cpu_baseline(sample_iters=args.cpu_iters)
         cpu_per = base["s_per_iter"] * it64
@@ -316,11 +382,13 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--nsrc", type=int, default=8)
-    ap.add_argument("--prec", default="half", choices=["half", "single", "double"])
+    # defaults: the fastest measured configuration per solved source on GB300
+    ap.add_argument("--nsrc", type=int, default=4)
+    ap.add_argument("--prec", default="single", choices=["half", "single", "double"])
     ap.add_argument("--cpu-iters", type=int, default=12)
     ap.add_argument("--ref-iters", type=int, default=int(os.environ.get("MKS_REF_ITERS", "0")) or None)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         if args.ref_iters is None:
