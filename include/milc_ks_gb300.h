@@ -231,6 +231,16 @@ int mks_load_hisq_aux(const double *U, const double *V, const double *W);
 int mks_fermion_force_multi_hisq(double eps, const double *residues,
                                  const double *const *xxx, int nterms,
                                  const int *n_orders_naik, int n_naiks, double *mom);
+/* asqtad fermion force.  Replaces eo_fermion_force_multi of an asqtad
+ * build (generic_ks/fermion_force_multi.c:29-44 -> fermion_force_fn_multi,
+ * generic_ks/fermion_force_fn_multi.c:80-316; GPU wrapper
+ * generic_ks/fermion_force_asqtad_gpu.c): mom[dir](x) <- TA(mom + 2 eps
+ * U_mu(x) dS/dU_mu(x)) through the asqtad fat + Naik links (tadpole factor
+ * u0 of the last mks_load_links_from_thin with MKS_ACTION_ASQTAD; no
+ * unitarization), xxx_j and residues as for the HISQ force.  Returns
+ * MKS_ERR_STATE unless asqtad links were loaded from thin links. */
+int mks_fermion_force_multi_asqtad(double eps, const double *residues,
+                                   const double *const *xxx, int nterms, double *mom);
 /* FP64 flops of the adjoint kernels in the last force call (our count:
    198 per 3x3 complex matrix product), and the number of links where the
    eigenvalue filter (generic_ks/su3_mat_op.c:1680-1734) was applied. */

@@ -12,6 +12,7 @@ this module                    MILC (generic_ks)
 =============================  ==============================================
 ``dslash_fn_field``            dslash_fn.c:348 / dslash_fn_dblstore.c:285
 ``ks_congrad_parity``          d_congrad5_fn_milc.c:61 (ks_congrad_parity_gpu)
+``ks_congrad_field``           d_congrad5.c:334
 ``ks_congrad_block_parity``    d_congrad5_fn_gpu.c:167
 ``mat_invert_uml_field``       mat_invert.c:328
 ``mat_invert_block_uml``       mat_invert.c:409
@@ -30,6 +31,7 @@ from ._lib import (MKS_EVEN as EVEN, MKS_ODD as ODD, MKS_EVENANDODD as EVENANDOD
 
 __all__ = ["EVEN", "ODD", "EVENANDODD", "PREC_HALF", "PREC_SINGLE", "PREC_DOUBLE", "QuarkInvertControl",
            "init", "set_lattice", "load_fn_links", "get_fn_links", "dslash_fn_field", "ks_congrad_parity",
+           "ks_congrad_field",
            "ks_congrad_block_parity", "mat_invert_uml_field", "mat_invert_block_uml",
            "ks_multicg_offset_field", "ks_ratinv", "ks_rateval", "load_hisq_links", "load_asqtad_links", "get_hisq_aux",
            "eo_fermion_force_multi", "gen_thin_links", "apply_phases", "gen_vector", "gen_momenta",
@@ -111,6 +113,21 @@ def ks_congrad_parity(src, dest, qic, mass, fn=0):
 
 def _pp(arrs):
     return (_lib.DP * len(arrs))(*[_dp(a) for a in arrs])
+
+
+def ks_congrad_field(src, dest, qic, mass, fn=0):
+    """generic_ks/d_congrad5.c:334-364: qic.parity EVEN, ODD or EVENANDODD
+    (the even solve, then the odd one); returns the summed iterations."""
+    parity = qic.parity
+    iters = 0
+    for par in (EVEN, ODD):
+        if parity == par or parity == EVENANDODD:
+            qic.parity = par
+            try:
+                iters += ks_congrad_parity(src, dest, qic, mass, fn)
+            finally:
+                qic.parity = parity
+    return iters
 
 
 def ks_congrad_block_parity(src, dest, qic, mass, fn=0):
@@ -196,8 +213,15 @@ def get_hisq_aux():
     return Vl, W
 
 
-def eo_fermion_force_multi(eps, residues, xxx, mom, n_orders_naik=None, n_naiks=1):
+def eo_fermion_force_multi(eps, residues, xxx, mom, n_orders_naik=None, n_naiks=1, action="hisq"):
+    """mom updated in place.  action "hisq": fermion_force_hisq_multi.c:170;
+    "asqtad": fermion_force_multi.c:29 (FNMAT, fermion_force_fn_multi.c:80),
+    which needs links loaded with load_asqtad_links."""
     res = np.ascontiguousarray(residues, dtype=np.float64)
+    if action == "asqtad":
+        check(init().mks_fermion_force_multi_asqtad(eps, _dp(res), _pp(list(xxx)), len(res), _dp(mom)),
+              "mks_fermion_force_multi_asqtad")
+        return mom
     n = len(res)
     if n_orders_naik is None:
         n_orders_naik = [n] + [0] * (n_naiks - 1)

@@ -106,18 +106,31 @@ void capture_account(const Capture &k) {
   }
 }
 
+// Scratch for a reduction of nsum sums per block over `blocks` blocks
+// (grid_reduce_last in mks_reduce.cuh): block rows + group rows, and the
+// top counter + one counter per group.  Grown, never shrunk; counters are
+// zeroed when (re)allocated and are left at zero by every launch.
 int ensure_red(int nsum, int blocks) {
   Context &c = g_ctx;
-  size_t need = (size_t)nsum * blocks;
-  if ((size_t)c.red.max_blocks >= need) return MKS_OK;
-  dev_free(c.red.partials);
-  size_t n = need < 65536 ? 65536 : need;
-  MKS_TRY(dev_alloc((void **)&c.red.partials, n * sizeof(double)));
-  if (!c.red.count) {
-    MKS_TRY(dev_alloc((void **)&c.red.count, 64 * sizeof(unsigned int)));
-    MKS_CUDA(cudaMemsetAsync(c.red.count, 0, 64 * sizeof(unsigned int), c.stream));
+  const size_t ngroups = ((size_t)blocks + RED_GROUP - 1) / RED_GROUP;
+  const size_t need = (size_t)nsum * ((size_t)blocks + ngroups), need_count = 1 + ngroups;
+  if (c.red.max_partials < need) {
+    dev_free(c.red.partials);
+    c.red.partials = nullptr;
+    c.red.max_partials = 0;
+    const size_t n = need < 65536 ? 65536 : need;
+    MKS_TRY(dev_alloc((void **)&c.red.partials, n * sizeof(double)));
+    c.red.max_partials = n;
   }
-  c.red.max_blocks = (int)n;
+  if (c.red.max_count < need_count) {
+    dev_free(c.red.count);
+    c.red.count = nullptr;
+    c.red.max_count = 0;
+    const size_t n = need_count < 4096 ? 4096 : need_count;
+    MKS_TRY(dev_alloc((void **)&c.red.count, n * sizeof(unsigned int)));
+    MKS_CUDA(cudaMemsetAsync(c.red.count, 0, n * sizeof(unsigned int), c.stream));
+    c.red.max_count = n;
+  }
   return MKS_OK;
 }
 

@@ -172,7 +172,7 @@ k_dslash(const LinkT fat, const LinkT lng, const DslashArgs<InT, OutT, typename 
   if (NSUM > 0) {
     __shared__ double smem[(256 / 32 + 1) * MAXSRC * 3];
     __shared__ double tot[MAXSRC * 3];
-    __shared__ double scratch[32];
+    __shared__ double scratch[256];
     block_reduce_grouped<R, NB, (NSUM > 0 ? NSUM : 1)>(sums, G, smem);
     const int nslots = G * NB;
     const double *btot = smem + (blockDim.x >> 5) * nslots * NSUM;

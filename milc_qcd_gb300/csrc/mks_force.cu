@@ -446,6 +446,74 @@ int force_dev(double eps, const double *residues, double2 *const *xs, int nterms
   return rc;
 }
 
+// asqtad (generic_ks/fermion_force_fn_multi.c:80-316): one smearing
+// level, the fat and Naik links built from the thin links U with the
+// tadpole-improved coefficients and no projection, so K_U is the fat-link
+// adjoint plus the Naik adjoint of the level-0 outer products.
+int force_asqtad_dev(double eps, const double *residues, double2 *const *xs, int nterms, double *mom_dev) {
+  Context &c = ctx();
+  const size_t Vh = c.Vh, nl = 8 * 9 * Vh, nm = 2 * 9 * Vh;
+  g_force_flops = 0.0;
+  g_nfilter = 0;
+  const double u2 = c.aux_u0 * c.aux_u0, u4 = u2 * u2, u6 = u4 * u2;
+  // asqtad_action.h with the tadpole division of ks_action_paths.c
+  const ForceCoeffs ca = {1.0 / 8.0 + 6.0 / 16.0 + 1.0 / 8.0, -1.0 / 24.0 / u2, -1.0 / 16.0 / u2, 1.0 / 64.0 / u4,
+                          -1.0 / 384.0 / u6, -1.0 / 16.0 / u4};
+  double2 *buf = nullptr;
+  MKS_TRY(dev_alloc((void **)&buf, (3 * nl + 4 * nm) * sizeof(double2)));
+  double2 *Kf = buf, *Kl = Kf + nl, *KU = Kl + nl;
+  double2 *S1 = KU + nl, *S2 = S1 + nm, *K1 = S2 + nm, *K2 = K1 + nm;
+  int rc = MKS_OK;
+  do {
+    if (cudaMemsetAsync(buf, 0, 3 * nl * sizeof(double2), c.stream) != cudaSuccess) { rc = MKS_ERR_CUDA; break; }
+    OuterArgs oa;
+    memset(&oa, 0, sizeof oa);
+    for (int j = 0; j < nterms; j++) { oa.x[j] = xs[j]; oa.res[j] = residues[j]; }
+    oa.j0 = 0; oa.j1 = nterms; oa.scale = 1.0;
+    if ((rc = outer(oa, Kf, Kl)) < 0) break;
+    if ((rc = fat_adj(c.auxU, ca, Kf, KU, S1, S2, K1, K2)) < 0) break;
+    if ((rc = naik_adj(c.auxU, Kl, KU, ca.naik)) < 0) break;
+    timing_begin(MKS_K_FORCE);
+    k_force_mom<<<dim3(grid_for(Vh, 128), 2, 4), 128, 0, c.stream>>>(c.geom, c.auxU, KU, mom_dev, 2.0 * eps);
+    timing_end(MKS_K_FORCE);
+    if (cudaGetLastError() != cudaSuccess) { rc = MKS_ERR_CUDA; break; }
+    if (cudaStreamSynchronize(c.stream) != cudaSuccess) rc = MKS_ERR_CUDA;
+  } while (0);
+  dev_free(buf);
+  return rc;
+}
+
+// Host staging shared by the force entry points: xxx[j] (MILC AoS, both
+// parities) to device SoA FP64, mom (anti_hermitmat[V][4]) to the device
+// and back around run(xs, mom_dev).
+template <class Run>
+static int force_host(const double *const *xxx, int nterms, double *mom, const Run &run) {
+  Context &c = ctx();
+  const size_t vbytes = c.V * 6 * sizeof(double), mbytes = c.V * 40 * sizeof(double);
+  double *stage = nullptr;
+  double2 *xs = nullptr;
+  double *mom_dev = nullptr;
+  MKS_TRY(dev_alloc((void **)&stage, vbytes));
+  int rc = dev_alloc((void **)&xs, (size_t)nterms * 6 * c.V * sizeof(double2) / 2);
+  if (rc >= 0) rc = dev_alloc((void **)&mom_dev, mbytes);
+  std::vector<double2 *> xp(nterms);
+  for (int j = 0; j < nterms && rc >= 0; j++) {
+    xp[j] = xs + (size_t)j * 6 * c.Vh;
+    if (cudaMemcpyAsync(stage, xxx[j], vbytes, cudaMemcpyHostToDevice, c.stream) != cudaSuccess) rc = MKS_ERR_CUDA;
+    if (rc >= 0) rc = vec_aos_to_soa64(stage, xp[j], 0);
+    if (rc >= 0) rc = vec_aos_to_soa64(stage, xp[j] + 3 * c.Vh, 1);
+    if (rc >= 0 && cudaStreamSynchronize(c.stream) != cudaSuccess) rc = MKS_ERR_CUDA;
+  }
+  if (rc >= 0 && cudaMemcpyAsync(mom_dev, mom, mbytes, cudaMemcpyHostToDevice, c.stream) != cudaSuccess)
+    rc = MKS_ERR_CUDA;
+  if (rc >= 0) rc = run(xp.data(), mom_dev);
+  if (rc >= 0 && cudaMemcpyAsync(mom, mom_dev, mbytes, cudaMemcpyDeviceToHost, c.stream) != cudaSuccess)
+    rc = MKS_ERR_CUDA;
+  if (rc >= 0 && cudaStreamSynchronize(c.stream) != cudaSuccess) rc = MKS_ERR_CUDA;
+  dev_free(stage); dev_free(xs); dev_free(mom_dev);
+  return rc;
+}
+
 }  // namespace mks
 
 using namespace mks;
@@ -469,29 +537,21 @@ int mks_fermion_force_multi_hisq(double eps, const double *residues, const doubl
   if (tot != nterms) return MKS_ERR_ARG;
   for (int i = 1; i < n_naiks; i++)
     if (!c.slots[i].valid) return MKS_ERR_STATE;
-  const size_t vbytes = c.V * 6 * sizeof(double), mbytes = c.V * 40 * sizeof(double);
-  double *stage = nullptr;
-  double2 *xs = nullptr;
-  double *mom_dev = nullptr;
-  MKS_TRY(dev_alloc((void **)&stage, vbytes));
-  int rc = dev_alloc((void **)&xs, (size_t)nterms * 6 * c.V * sizeof(double2) / 2);
-  if (rc >= 0) rc = dev_alloc((void **)&mom_dev, mbytes);
-  std::vector<double2 *> xp(nterms);
-  for (int j = 0; j < nterms && rc >= 0; j++) {
-    xp[j] = xs + (size_t)j * 6 * c.Vh;
-    if (cudaMemcpyAsync(stage, xxx[j], vbytes, cudaMemcpyHostToDevice, c.stream) != cudaSuccess) rc = MKS_ERR_CUDA;
-    if (rc >= 0) rc = vec_aos_to_soa64(stage, xp[j], 0);
-    if (rc >= 0) rc = vec_aos_to_soa64(stage, xp[j] + 3 * c.Vh, 1);
-    if (rc >= 0 && cudaStreamSynchronize(c.stream) != cudaSuccess) rc = MKS_ERR_CUDA;
-  }
-  if (rc >= 0 && cudaMemcpyAsync(mom_dev, mom, mbytes, cudaMemcpyHostToDevice, c.stream) != cudaSuccess)
-    rc = MKS_ERR_CUDA;
-  if (rc >= 0) rc = force_dev(eps, residues, xp.data(), nterms, n_orders_naik, n_naiks, mom_dev);
-  if (rc >= 0 && cudaMemcpyAsync(mom, mom_dev, mbytes, cudaMemcpyDeviceToHost, c.stream) != cudaSuccess)
-    rc = MKS_ERR_CUDA;
-  if (rc >= 0 && cudaStreamSynchronize(c.stream) != cudaSuccess) rc = MKS_ERR_CUDA;
-  dev_free(stage); dev_free(xs); dev_free(mom_dev);
-  return rc;
+  if (c.aux_action != MKS_ACTION_HISQ) return MKS_ERR_STATE;
+  return force_host(xxx, nterms, mom, [&](double2 *const *xs, double *mom_dev) {
+    return force_dev(eps, residues, xs, nterms, n_orders_naik, n_naiks, mom_dev);
+  });
+}
+
+int mks_fermion_force_multi_asqtad(double eps, const double *residues, const double *const *xxx, int nterms,
+                                   double *mom) {
+  MKS_TRY(check_ready());
+  Context &c = ctx();
+  if (!c.auxU || c.aux_action != MKS_ACTION_ASQTAD) return MKS_ERR_STATE;
+  if (nterms <= 0 || nterms > 64 || !residues || !xxx || !mom) return MKS_ERR_ARG;
+  return force_host(xxx, nterms, mom, [&](double2 *const *xs, double *mom_dev) {
+    return force_asqtad_dev(eps, residues, xs, nterms, mom_dev);
+  });
 }
 
 double mks_force_flops_last(void) { return g_force_flops; }

@@ -262,11 +262,15 @@ struct LinkF16 {
 };
 
 // ------------------------------------------------------------------
-// device-side reduction scratch: per-block partials + arrival counter
+// device-side reduction scratch for grid_reduce_last: per-block and
+// per-group rows of partial sums, and the arrival counters (top + one per
+// group of blocks), which return to 0 at the end of every launch
+constexpr int RED_GROUP = 64;  // blocks per first-level group
 struct RedScratch {
-  double *partials;     // [nsum][max_blocks]
-  unsigned int *count;  // arrival counter, returns to 0 after each use
-  int max_blocks;
+  double *partials;     // capacity: max_partials doubles
+  unsigned int *count;  // capacity: max_count counters
+  size_t max_partials;
+  size_t max_count;
 };
 
 // ------------------------------------------------------------------
@@ -292,8 +296,12 @@ struct Context {
   Geom geom{};
   LinkSlot slots[MKS_MAX_SLOTS];
   RedScratch red{};
-  // HISQ auxiliary links (FP64, device, [2][4][9][Vh] SoA like fat64)
+  // thin links (auxU, phases in) and the HISQ smearing stages V, W (FP64,
+  // device, [2][4][9][Vh] SoA like fat64), with the action and tadpole
+  // factor the fat/long links of slot 0 were built with (0: unknown)
   double2 *auxU = nullptr, *auxV = nullptr, *auxW = nullptr;
+  int aux_action = 0;
+  double aux_u0 = 1.0;
   // timing
   bool timing = false;
   double kernel_ms[MKS_K_COUNT] = {0};

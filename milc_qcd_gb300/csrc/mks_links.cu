@@ -247,6 +247,8 @@ int links_from_thin(int action, const double *thin_dev_aos, int n_naiks, const d
     s.eps_naik = eps_naik ? eps_naik[i] : 0.0;
     s.valid = true;
   }
+  c.aux_action = action;
+  c.aux_u0 = u0;
   MKS_CUDA(cudaMemcpyAsync(&g_nsvd, nsvd, sizeof(unsigned int), cudaMemcpyDeviceToHost, c.stream));
   MKS_CUDA(cudaStreamSynchronize(c.stream));
   dev_free(nsvd); dev_free(staple); dev_free(tmp); dev_free(f3); dev_free(l3);
@@ -370,6 +372,8 @@ int mks_hisq_aux_links(const double coeffs1[6], const double *U, double *V, doub
   if (rc >= 0 && cudaMemcpyAsync(stage, U, bytes, cudaMemcpyHostToDevice, c.stream) != cudaSuccess)
     rc = MKS_ERR_CUDA;
   if (rc >= 0) rc = links_aos_to_soa64(stage, c.auxU);
+  c.aux_action = MKS_ACTION_HISQ;
+  c.aux_u0 = 1.0;
   if (rc >= 0) rc = fatten(c.auxU, cf, c.auxV, S, T);
   if (rc >= 0) {
     timing_begin(MKS_K_LINKS);
@@ -396,6 +400,8 @@ int mks_load_hisq_aux(const double *U, const double *V, const double *W) {
   MKS_TRY(dev_alloc((void **)&stage, bytes));
   const double *src[3] = {U, V, W};
   double2 *dst[3] = {c.auxU, c.auxV, c.auxW};
+  c.aux_action = MKS_ACTION_HISQ;
+  c.aux_u0 = 1.0;
   int rc = MKS_OK;
   for (int k = 0; k < 3 && rc >= 0; k++) {
     if (cudaMemcpyAsync(stage, src[k], bytes, cudaMemcpyHostToDevice, c.stream) != cudaSuccess) rc = MKS_ERR_CUDA;

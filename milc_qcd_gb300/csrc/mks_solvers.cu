@@ -325,7 +325,7 @@ static int launch_site(int family, const Op &op, const Fin &fin, const int *skip
   if (gx > cap) gx = cap;
   MKS_TRY(ensure_red(NSUM > 0 ? NSUM * nsrc : 1, gx));
   timing_begin(family);
-  k_site<Op, NSUM, Fin><<<dim3(gx, nsrc), 256, 0, c.stream>>>(op, fin, skip, Vh, c.red.partials, c.red.count + 1,
+  k_site<Op, NSUM, Fin><<<dim3(gx, nsrc), 256, 0, c.stream>>>(op, fin, skip, Vh, c.red.partials, c.red.count,
                                                              totals);
   timing_end(family);
   MKS_CUDA(cudaGetLastError());

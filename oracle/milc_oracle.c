@@ -539,14 +539,18 @@ int orc_u3_unitarize(const double *V, double *W) {
 
 /* asqtad: generic_ks/imp_actions/asqtad_action.h:22-47 with the tadpole
    division of ks_action_paths.c (coefficient / u0^(length-1)) */
+void orc_asqtad_coeffs(double u0, orc_coeffs *c) {
+  c->one_link = (1.0 / 8.0) + (6.0 / 16.0) + (1.0 / 8.0);
+  c->naik = (-1.0 / 24.0) / (u0 * u0);
+  c->three_staple = (-1.0 / 8.0) * 0.5 / (u0 * u0);
+  c->five_staple = (1.0 / 8.0) * 0.25 * 0.5 / (u0 * u0 * u0 * u0);
+  c->seven_staple = (-1.0 / 8.0) * 0.125 * (1.0 / 6.0) / (u0 * u0 * u0 * u0 * u0 * u0);
+  c->lepage = (-1.0 / 16) / (u0 * u0 * u0 * u0);
+}
+
 void orc_asqtad_links(const orc_lat *L, const double *U, double u0, double *fat, double *lng) {
   orc_coeffs c;
-  c.one_link = (1.0 / 8.0) + (6.0 / 16.0) + (1.0 / 8.0);
-  c.naik = (-1.0 / 24.0) / (u0 * u0);
-  c.three_staple = (-1.0 / 8.0) * 0.5 / (u0 * u0);
-  c.five_staple = (1.0 / 8.0) * 0.25 * 0.5 / (u0 * u0 * u0 * u0);
-  c.seven_staple = (-1.0 / 8.0) * 0.125 * (1.0 / 6.0) / (u0 * u0 * u0 * u0 * u0 * u0);
-  c.lepage = (-1.0 / 16) / (u0 * u0 * u0 * u0);
+  orc_asqtad_coeffs(u0, &c);
   orc_load_fatlinks(L, U, &c, fat);
   orc_load_lnglinks(L, U, &c, lng);
 }

@@ -52,10 +52,15 @@ int orc_multicg_offset(const orc_lat *L, const double *fat, const double *lng,
 void orc_load_fatlinks(const orc_lat *L, const double *links, const orc_coeffs *c, double *fat);
 void orc_load_lnglinks(const orc_lat *L, const double *links, const orc_coeffs *c, double *lng);
 int orc_u3_unitarize(const double *V, double *W);
+void orc_asqtad_coeffs(double u0, orc_coeffs *c);
 void orc_asqtad_links(const orc_lat *L, const double *U, double u0, double *fat, double *lng);
 int orc_hisq_links(const orc_lat *L, const double *U, int n_naiks, const double *eps_naik,
                    double *Vl, double *W, double *fat, double *lng);
 
+/* asqtad force, generic_ks/fermion_force_fn_multi.c:80-316 (FNMAT):
+   mom <- TA(mom + 2 eps U K_U) through the asqtad fat + Naik links of U */
+void orc_fermion_force_asqtad(const orc_lat *L, const double *U, double u0, double eps,
+                              const double *residues, const double *xxx, int nterms, double *mom);
 void orc_fermion_force_hisq(const orc_lat *L, const double *U, int n_naiks,
                             const double *eps_naik, double eps, const double *residues,
                             const double *xxx, int nterms, const int *n_orders_naik,

@@ -312,12 +312,7 @@ static int force_KU(const orc_lat *L, const double *U, int n_naiks, const double
 
 /* mom <- TA(mom + FACTOR eps U K_U) in MILC's anti_hermitmat layout
    (libraries/make_ahmat.c, uncmp_ahmat.c) */
-void orc_fermion_force_hisq(const orc_lat *L, const double *U, int n_naiks, const double *eps_naik,
-                            double eps, const double *residues, const double *xxx, int nterms,
-                            const int *n_orders_naik, double *mom) {
-  size_t nl = L->V * 4 * 18;
-  double *KU = malloc(nl * sizeof(double));
-  force_KU(L, U, n_naiks, eps_naik, residues, xxx, nterms, n_orders_naik, KU);
+static void mom_update(const orc_lat *L, const double *U, const double *KU, double eps, double *mom) {
   for (size_t x = 0; x < L->V; x++)
     for (int mu = 0; mu < 4; mu++) {
       double G[18];
@@ -340,7 +335,37 @@ void orc_fermion_force_hisq(const orc_lat *L, const double *U, int n_naiks, cons
       m[2] = (RE(A, 0, 2) - RE(A, 2, 0)) * 0.5; m[3] = (IM(A, 0, 2) + IM(A, 2, 0)) * 0.5;
       m[4] = (RE(A, 1, 2) - RE(A, 2, 1)) * 0.5; m[5] = (IM(A, 1, 2) + IM(A, 2, 1)) * 0.5;
     }
+}
+
+void orc_fermion_force_hisq(const orc_lat *L, const double *U, int n_naiks, const double *eps_naik,
+                            double eps, const double *residues, const double *xxx, int nterms,
+                            const int *n_orders_naik, double *mom) {
+  size_t nl = L->V * 4 * 18;
+  double *KU = malloc(nl * sizeof(double));
+  force_KU(L, U, n_naiks, eps_naik, residues, xxx, nterms, n_orders_naik, KU);
+  mom_update(L, U, KU, eps, mom);
   free(KU);
+}
+
+/* asqtad: one smearing level, fat + Naik links built directly from U with
+   the tadpole-improved coefficients and no unitarization, so K_U is the
+   fat-link adjoint plus the Naik adjoint of the level-0 outer products.
+   MILC walks its sorted path table (fermion_force_fn_multi.c:145-297,
+   forward paths doubled); the derivative is the same. */
+void orc_fermion_force_asqtad(const orc_lat *L, const double *U, double u0, double eps,
+                              const double *residues, const double *xxx, int nterms, double *mom) {
+  size_t nl = L->V * 4 * 18;
+  orc_coeffs c;
+  orc_asqtad_coeffs(u0, &c);
+  double *Kf = calloc(nl, sizeof(double)), *Kl = calloc(nl, sizeof(double)), *KU = calloc(nl, sizeof(double));
+  for (int j = 0; j < nterms; j++) {
+    outer(L, xxx + (size_t)j * 6 * L->V, residues[j], 1, Kf);
+    outer(L, xxx + (size_t)j * 6 * L->V, residues[j], 3, Kl);
+  }
+  fat_adj(L, U, &c, Kf, KU);
+  naik_adj(L, U, c.naik, Kl, KU);
+  mom_update(L, U, KU, eps, mom);
+  free(Kf); free(Kl); free(KU);
 }
 
 /* S_lin(U) = 2 Re sum_j res_j X_j^dag D_eo[links(U)] Y_j with X_j, Y_j the

@@ -160,6 +160,14 @@ class Oracle:
                                         ctypes.c_int(nterms), ords.ctypes.data_as(_ip), _ptr(mom))
         return mom
 
+    def fermion_force_asqtad(self, U, u0, eps, residues, xxx, mom=None):
+        res = np.ascontiguousarray(residues, dtype=np.float64)
+        xxx = np.ascontiguousarray(xxx, dtype=np.float64)
+        mom = np.zeros((self.V, 4, 10)) if mom is None else mom.copy()
+        self.lib.orc_fermion_force_asqtad(self.L, _ptr(U), ctypes.c_double(u0), ctypes.c_double(eps),
+                                          _ptr(res), _ptr(xxx), ctypes.c_int(len(res)), _ptr(mom))
+        return mom
+
     def force_action(self, U, residues, xxx, orders=None, eps_naik=(0.0,)):
         eps_arr = np.ascontiguousarray(eps_naik, dtype=np.float64)
         res = np.ascontiguousarray(residues, dtype=np.float64)
@@ -197,6 +205,9 @@ class MilcRef:
         c = np.zeros((self.V, 4), dtype=np.int32)
         self.lib.ref_coords(c.ctypes.data_as(_ip))
         return c
+
+    def set_u0(self, u0):
+        self.lib.ref_set_u0(ctypes.c_double(u0))
 
     def set_thin_links(self, U_unphased):
         self.lib.ref_set_thin_links(_ptr(np.ascontiguousarray(U_unphased)))

@@ -130,6 +130,12 @@ void ref_get_thin_links_phased(double *U) {
       memcpy(U + (4 * i + dir) * 18, &lattice[i].link[dir], 18 * sizeof(double));
 }
 
+/* Tadpole factor of the asqtad path coefficients (ks_action_paths.c divides
+   each coefficient by u0^(length-1)); set it before the first
+   ref_build_links / ref_fermion_force of the process, as MILC's force
+   caches its sorted path table on first use. */
+void ref_set_u0(double v) { u0 = v; }
+
 void ref_build_links(void) {
   if (fn_links != NULL) { REF_DESTROY_LINKS(fn_links); fn_links = NULL; }
   /* the DBLSTORE_FN dslash needs back links (ks_imp_rhmc/setup.c:581-584) */
@@ -243,22 +249,27 @@ int ref_multicg_offset(const double *src, double *psim, const double *offsets,
   return iters;
 }
 
-#if FERM_ACTION == HISQ
-/* HISQ fermion force.  xxx holds nterms vectors (X on even sites, D_oe X on
-   odd sites, as update_h_rhmc.c:82-87 prepares them); mom is read and
-   updated in place.  n_orders_naik[] gives the number of terms per Naik
-   epsilon group (first group includes every term with eps=0). */
+/* Fermion force (HISQ: fermion_force_hisq_multi.c; asqtad:
+   fermion_force_multi.c -> fermion_force_fn_multi.c).  xxx holds nterms
+   vectors (X on even sites, D_oe X on odd sites, as update_h_rhmc.c:82-87
+   prepares them); mom is read and updated in place.  For HISQ
+   n_orders_naik[] gives the number of terms per Naik epsilon group (first
+   group includes every term with eps=0); asqtad ignores it. */
 void ref_fermion_force(double eps, const double *residues, const double *xxx,
                        int nterms, const int *orders_naik, double *mom) {
   int j;
   size_t i;
   Real *res = (Real *)malloc(nterms * sizeof(Real));
   su3_vector **xv = (su3_vector **)malloc(nterms * sizeof(su3_vector *));
+#if FERM_ACTION == HISQ
   n_order_naik_total = 0;
   for (j = 0; j < ref_n_naiks; j++) {
     n_orders_naik[j] = orders_naik ? orders_naik[j] : (j == 0 ? nterms : 0);
     n_order_naik_total += n_orders_naik[j];
   }
+#else
+  (void)orders_naik;
+#endif
   for (j = 0; j < nterms; j++) {
     res[j] = residues[j];
     xv[j] = (su3_vector *)malloc(sites_on_node * sizeof(su3_vector));
@@ -272,6 +283,5 @@ void ref_fermion_force(double eps, const double *residues, const double *xxx,
   for (j = 0; j < nterms; j++) free(xv[j]);
   free(xv); free(res);
 }
-#endif
 
 int ref_sizeof_anti_hermitmat(void) { return (int)sizeof(anti_hermitmat); }
