@@ -78,7 +78,9 @@ class Clocks:
         sm = sorted(float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit())
         mx = max((float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()), default=None)
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > i + 2 and "Active" in s[i + 2]})
+        # nvidia-smi prints "Active" / "Not Active" per reason
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > i + 2 and s[i + 2].strip() == "Active"})
         return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons,
                 "samples": len(self.samples)}
 

@@ -241,6 +241,17 @@ int mks_fermion_force_multi_hisq(double eps, const double *residues,
  * MKS_ERR_STATE unless asqtad links were loaded from thin links. */
 int mks_fermion_force_multi_asqtad(double eps, const double *residues,
                                    const double *const *xxx, int nterms, double *mom);
+/* The backward half of the force as a forward/backward pair (no reference
+ * counterpart; MILC only ever applies the projected update): writes
+ * ku[4*i+dir] (su3_matrix layout, thin links of the last load with phases
+ * in) with dS = 2 Re sum_{x,mu} tr(K_U,mu(x) dU_mu(x)) for
+ * S = 2 Re sum_j residues[j] X_j^dag D_eo[links(U)] Y_j at fixed X_j (even
+ * part of xxx_j) and Y_j (odd part).  The forward half is D_eo itself on the
+ * links built from U.  Uses the action of the last mks_load_links_from_thin
+ * (or mks_load_hisq_aux: HISQ); n_orders_naik may be NULL when n_naiks is 1.
+ * The force entry points apply mom <- TA(mom + 2 eps U K_U). */
+int mks_fermion_force_adjoint(const double *residues, const double *const *xxx, int nterms,
+                              const int *n_orders_naik, int n_naiks, double *ku);
 /* FP64 flops of the adjoint kernels in the last force call (our count:
    198 per 3x3 complex matrix product), and the number of links where the
    eigenvalue filter (generic_ks/su3_mat_op.c:1680-1734) was applied. */

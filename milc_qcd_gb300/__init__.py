@@ -34,7 +34,7 @@ __all__ = ["EVEN", "ODD", "EVENANDODD", "PREC_HALF", "PREC_SINGLE", "PREC_DOUBLE
            "ks_congrad_field",
            "ks_congrad_block_parity", "mat_invert_uml_field", "mat_invert_block_uml",
            "ks_multicg_offset_field", "ks_ratinv", "ks_rateval", "load_hisq_links", "load_asqtad_links", "get_hisq_aux",
-           "eo_fermion_force_multi", "gen_thin_links", "apply_phases", "gen_vector", "gen_momenta",
+           "eo_fermion_force_multi", "fermion_force_adjoint", "gen_thin_links", "apply_phases", "gen_vector", "gen_momenta",
            "MksError"]
 
 
@@ -229,6 +229,19 @@ def eo_fermion_force_multi(eps, residues, xxx, mom, n_orders_naik=None, n_naiks=
     check(init().mks_fermion_force_multi_hisq(eps, _dp(res), _pp(list(xxx)), n, ords, n_naiks, _dp(mom)),
           "mks_fermion_force_multi_hisq")
     return mom
+
+
+def fermion_force_adjoint(residues, xxx, n_orders_naik=None, n_naiks=1):
+    """K_U (V, 4, 18) with dS = 2 Re sum tr(K_U dU) for the fermion bilinear
+    S = 2 Re sum_j residues[j] X_j^dag D_eo Y_j (X_j, Y_j the even / odd parts
+    of xxx[j]) through the links of the last load (mks_fermion_force_adjoint)."""
+    res = np.ascontiguousarray(residues, dtype=np.float64)
+    V = int(np.prod(_state["dims"]))
+    ku = np.zeros((V, 4, 18))
+    ords = None if n_orders_naik is None else (ctypes.c_int * len(n_orders_naik))(*n_orders_naik)
+    check(init().mks_fermion_force_adjoint(_dp(res), _pp(list(xxx)), len(res), ords, n_naiks, _dp(ku)),
+          "mks_fermion_force_adjoint")
+    return ku
 
 
 # ---- host-side synthetic inputs (no device work) ----

@@ -76,6 +76,7 @@ SIGNATURES = {
     "mks_load_hisq_aux": (ctypes.c_int, [DP, DP, DP]),
     "mks_fermion_force_multi_hisq": (ctypes.c_int, [ctypes.c_double, DP, DPP, ctypes.c_int, IP, ctypes.c_int, DP]),
     "mks_fermion_force_multi_asqtad": (ctypes.c_int, [ctypes.c_double, DP, DPP, ctypes.c_int, DP]),
+    "mks_fermion_force_adjoint": (ctypes.c_int, [DP, DPP, ctypes.c_int, IP, ctypes.c_int, DP]),
     "mks_force_flops_last": (ctypes.c_double, []),
     "mks_force_filter_count": (ctypes.c_int, []),
     "mks_timing_enable": (ctypes.c_int, [ctypes.c_int]),

@@ -389,8 +389,11 @@ static int outer(const OuterArgs &a, double2 *Kf, double2 *Kl) {
 
 static unsigned int g_nfilter = 0;
 
+// mom_dev: momentum updated in place; or, with ku_out set, K_U itself
+// (dS = 2 Re sum tr(K_U dU), [2][4][9][Vh] SoA) is copied there and mom_dev
+// is not touched.
 int force_dev(double eps, const double *residues, double2 *const *xs, int nterms, const int *orders, int n_naiks,
-              double *mom_dev) {
+              double *mom_dev, double2 *ku_out) {
   Context &c = ctx();
   const size_t Vh = c.Vh, nl = 8 * 9 * Vh, nm = 2 * 9 * Vh;
   g_force_flops = 0.0;
@@ -434,6 +437,12 @@ int force_dev(double eps, const double *residues, double2 *const *xs, int nterms
     g_force_flops += 20.0 * 198 * c.V * 4;
     if (cudaGetLastError() != cudaSuccess) { rc = MKS_ERR_CUDA; break; }
     if ((rc = fat_adj(c.auxU, c1, KV, KU, S1, S2, K1, K2)) < 0) break;
+    if (ku_out) {
+      if (cudaMemcpyAsync(ku_out, KU, nl * sizeof(double2), cudaMemcpyDeviceToDevice, c.stream) != cudaSuccess)
+        rc = MKS_ERR_CUDA;
+      if (rc >= 0 && cudaStreamSynchronize(c.stream) != cudaSuccess) rc = MKS_ERR_CUDA;
+      break;
+    }
     timing_begin(MKS_K_FORCE);
     k_force_mom<<<dim3(grid_for(Vh, 128), 2, 4), 128, 0, c.stream>>>(c.geom, c.auxU, KU, mom_dev, 2.0 * eps);
     timing_end(MKS_K_FORCE);
@@ -450,7 +459,8 @@ int force_dev(double eps, const double *residues, double2 *const *xs, int nterms
 // level, the fat and Naik links built from the thin links U with the
 // tadpole-improved coefficients and no projection, so K_U is the fat-link
 // adjoint plus the Naik adjoint of the level-0 outer products.
-int force_asqtad_dev(double eps, const double *residues, double2 *const *xs, int nterms, double *mom_dev) {
+int force_asqtad_dev(double eps, const double *residues, double2 *const *xs, int nterms, double *mom_dev,
+                     double2 *ku_out) {
   Context &c = ctx();
   const size_t Vh = c.Vh, nl = 8 * 9 * Vh, nm = 2 * 9 * Vh;
   g_force_flops = 0.0;
@@ -473,6 +483,12 @@ int force_asqtad_dev(double eps, const double *residues, double2 *const *xs, int
     if ((rc = outer(oa, Kf, Kl)) < 0) break;
     if ((rc = fat_adj(c.auxU, ca, Kf, KU, S1, S2, K1, K2)) < 0) break;
     if ((rc = naik_adj(c.auxU, Kl, KU, ca.naik)) < 0) break;
+    if (ku_out) {
+      if (cudaMemcpyAsync(ku_out, KU, nl * sizeof(double2), cudaMemcpyDeviceToDevice, c.stream) != cudaSuccess)
+        rc = MKS_ERR_CUDA;
+      if (rc >= 0 && cudaStreamSynchronize(c.stream) != cudaSuccess) rc = MKS_ERR_CUDA;
+      break;
+    }
     timing_begin(MKS_K_FORCE);
     k_force_mom<<<dim3(grid_for(Vh, 128), 2, 4), 128, 0, c.stream>>>(c.geom, c.auxU, KU, mom_dev, 2.0 * eps);
     timing_end(MKS_K_FORCE);
@@ -539,7 +555,7 @@ int mks_fermion_force_multi_hisq(double eps, const double *residues, const doubl
     if (!c.slots[i].valid) return MKS_ERR_STATE;
   if (c.aux_action != MKS_ACTION_HISQ) return MKS_ERR_STATE;
   return force_host(xxx, nterms, mom, [&](double2 *const *xs, double *mom_dev) {
-    return force_dev(eps, residues, xs, nterms, n_orders_naik, n_naiks, mom_dev);
+    return force_dev(eps, residues, xs, nterms, n_orders_naik, n_naiks, mom_dev, nullptr);
   });
 }
 
@@ -550,8 +566,52 @@ int mks_fermion_force_multi_asqtad(double eps, const double *residues, const dou
   if (!c.auxU || c.aux_action != MKS_ACTION_ASQTAD) return MKS_ERR_STATE;
   if (nterms <= 0 || nterms > 64 || !residues || !xxx || !mom) return MKS_ERR_ARG;
   return force_host(xxx, nterms, mom, [&](double2 *const *xs, double *mom_dev) {
-    return force_asqtad_dev(eps, residues, xs, nterms, mom_dev);
+    return force_asqtad_dev(eps, residues, xs, nterms, mom_dev, nullptr);
   });
+}
+
+int mks_fermion_force_adjoint(const double *residues, const double *const *xxx, int nterms,
+                              const int *n_orders_naik, int n_naiks, double *ku) {
+  MKS_TRY(check_ready());
+  Context &c = ctx();
+  if (!c.auxU || (c.aux_action != MKS_ACTION_HISQ && c.aux_action != MKS_ACTION_ASQTAD)) return MKS_ERR_STATE;
+  if (nterms <= 0 || nterms > 64 || !residues || !xxx || !ku) return MKS_ERR_ARG;
+  const bool hisq = c.aux_action == MKS_ACTION_HISQ;
+  std::vector<int> one(1, nterms);
+  if (hisq) {
+    if (n_naiks < 1 || n_naiks > MKS_MAX_SLOTS) return MKS_ERR_ARG;
+    if (!n_orders_naik) {
+      if (n_naiks != 1) return MKS_ERR_ARG;
+      n_orders_naik = one.data();
+    }
+    int tot = 0;
+    for (int i = 0; i < n_naiks; i++) {
+      if (n_orders_naik[i] < 0) return MKS_ERR_ARG;
+      tot += n_orders_naik[i];
+    }
+    if (tot != nterms) return MKS_ERR_ARG;
+    for (int i = 1; i < n_naiks; i++)
+      if (!c.slots[i].valid) return MKS_ERR_STATE;
+  }
+  const size_t nl = 8 * 9 * c.Vh;
+  double2 *kd = nullptr;
+  double *stage = nullptr, *mom = nullptr;
+  MKS_TRY(dev_alloc((void **)&kd, nl * sizeof(double2)));
+  int rc = dev_alloc((void **)&stage, nl * sizeof(double2));
+  // force_host stages a momentum field; it is not used when K_U is asked for
+  std::vector<double> mom_host;
+  if (rc >= 0) { mom_host.assign(c.V * 40, 0.0); mom = mom_host.data(); }
+  if (rc >= 0)
+    rc = force_host(xxx, nterms, mom, [&](double2 *const *xs, double *mom_dev) {
+      return hisq ? force_dev(1.0, residues, xs, nterms, n_orders_naik, n_naiks, mom_dev, kd)
+                  : force_asqtad_dev(1.0, residues, xs, nterms, mom_dev, kd);
+    });
+  if (rc >= 0) rc = links_soa64_to_aos(kd, stage);
+  if (rc >= 0 && cudaMemcpyAsync(ku, stage, nl * sizeof(double2), cudaMemcpyDeviceToHost, c.stream) != cudaSuccess)
+    rc = MKS_ERR_CUDA;
+  if (rc >= 0 && cudaStreamSynchronize(c.stream) != cudaSuccess) rc = MKS_ERR_CUDA;
+  dev_free(kd); dev_free(stage);
+  return rc;
 }
 
 double mks_force_flops_last(void) { return g_force_flops; }
