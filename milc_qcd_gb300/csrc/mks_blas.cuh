@@ -15,7 +15,7 @@ constexpr int BLAS_MAXSRC = 16;
 
 template <class Op, int NSUM, class Fin>
 __global__ void __launch_bounds__(256) k_site(const Op op, const Fin fin, const int *skip, int Vh,
-                                              double *partials, unsigned int *count, double *totals) {
+                                              const RedScratch red, double *totals) {
   if (skip && *skip) return;
   constexpr int NS = NSUM > 0 ? NSUM : 1;
   const int s = blockIdx.y;
@@ -50,7 +50,7 @@ __global__ void __launch_bounds__(256) k_site(const Op op, const Fin fin, const 
   }
   __syncthreads();
   // each block's row carries its own source's NS sums and zeros elsewhere
-  if (!grid_reduce_last(row, n, partials, count, tot, scratch)) return;
+  if (!grid_reduce_last(row, n, red, tot, scratch)) return;
   if (threadIdx.x == 0 && totals)
     for (int i = 0; i < n; i++) totals[i] = tot[i];
   __syncthreads();

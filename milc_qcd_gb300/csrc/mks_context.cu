@@ -122,6 +122,10 @@ int ensure_red(int nsum, int blocks) {
     MKS_TRY(dev_alloc((void **)&c.red.partials, n * sizeof(double)));
     c.red.max_partials = n;
   }
+  if (!c.red.err) {
+    MKS_TRY(dev_alloc((void **)&c.red.err, sizeof(int)));
+    MKS_CUDA(cudaMemsetAsync(c.red.err, 0, sizeof(int), c.stream));
+  }
   if (c.red.max_count < need_count) {
     dev_free(c.red.count);
     c.red.count = nullptr;
@@ -132,6 +136,18 @@ int ensure_red(int nsum, int blocks) {
     c.red.max_count = n;
   }
   return MKS_OK;
+}
+
+int red_check() {
+  Context &c = g_ctx;
+  if (!c.red.err) return MKS_OK;
+  int e = 0;
+  MKS_CUDA(cudaMemcpyAsync(&e, c.red.err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  MKS_CUDA(cudaStreamSynchronize(c.stream));
+  if (!e) return MKS_OK;
+  MKS_CUDA(cudaMemsetAsync(c.red.err, 0, sizeof(int), c.stream));
+  snprintf(g_errmsg, sizeof g_errmsg, "reduction scratch too small for a launch (internal sizing error)");
+  return MKS_ERR_CUDA;
 }
 
 // ---------------- layout conversion kernels ----------------
@@ -371,7 +387,7 @@ int mks_finalize(void) {
   if (!c.initialised) return MKS_OK;
   cudaStreamSynchronize(c.stream);
   free_lattice_fields();
-  dev_free(c.red.partials); dev_free(c.red.count);
+  dev_free(c.red.partials); dev_free(c.red.count); dev_free(c.red.err);
   c.red = RedScratch();
   for (auto &e : c.ev_pool) cudaEventDestroy(e);
   c.ev_pool.clear();
@@ -399,6 +415,13 @@ int mks_set_lattice(const int dims[4]) {
   c.geom.nx = dims[0]; c.geom.ny = dims[1]; c.geom.nz = dims[2]; c.geom.nt = dims[3];
   c.geom.Vh = (int)c.Vh;
   c.geom.sx = 1; c.geom.sy = dims[0]; c.geom.sz = dims[0] * dims[1]; c.geom.st = dims[0] * dims[1] * dims[2];
+  // Reduction scratch for the largest reducing launch on this lattice, so
+  // that it is never reallocated while a solver batch is being captured:
+  // D_eo epilogues (up to 16 threads per site in blocks of >= 128 threads,
+  // 16 sources x 3 sums) and the BLAS site kernels (up to 4 blocks per SM
+  // per source row, 32 rows x 3 sums).
+  MKS_TRY(ensure_red(16 * 3, (int)((c.Vh * 16 + 127) / 128)));
+  MKS_TRY(ensure_red(32 * 3, c.sm_count * 4 * 32));
   return MKS_OK;
 }
 

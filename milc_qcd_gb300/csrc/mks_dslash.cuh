@@ -36,8 +36,7 @@ struct DslashArgs {
   double coef[MAXSRC];
   const int *skip;            // kernel returns at once when *skip != 0
   const int *src_done;        // per-source: skip the epilogue update when non-zero
-  double *partials;
-  unsigned int *count;
+  RedScratch red;             // grid reduction scratch (NSUM > 0)
   double *totals;             // [nsrc][NSUM] written by the last block
 };
 
@@ -176,7 +175,7 @@ k_dslash(const LinkT fat, const LinkT lng, const DslashArgs<InT, OutT, typename 
     block_reduce_grouped<R, NB, (NSUM > 0 ? NSUM : 1)>(sums, G, smem);
     const int nslots = G * NB;
     const double *btot = smem + (blockDim.x >> 5) * nslots * NSUM;
-    if (grid_reduce_last(btot, nslots * NSUM, a.partials, a.count, tot, scratch)) {
+    if (grid_reduce_last(btot, nslots * NSUM, a.red, tot, scratch)) {
       if (threadIdx.x == 0) {
         for (int i = 0; i < a.nsrc * NSUM; i++) a.totals[i] = tot[i];
       }

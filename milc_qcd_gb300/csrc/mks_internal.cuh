@@ -271,7 +271,9 @@ struct RedScratch {
   unsigned int *count;  // capacity: max_count counters
   size_t max_partials;
   size_t max_count;
+  int *err;             // set on the device when a launch would overrun the scratch
 };
+int red_check();  // MKS_ERR_CUDA (and clears the flag) if a reduction overran
 
 // ------------------------------------------------------------------
 // host-side context

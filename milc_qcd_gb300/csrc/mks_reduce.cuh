@@ -87,29 +87,40 @@ __device__ __forceinline__ void sum_rows(const double *rows, int nrows, int n, d
 // depend on block scheduling.  Returns true in the one block that holds
 // the grid totals in out[0..n) (shared) on return.
 //
-// partials: (nblocks + ngroups) * n doubles; count: 1 + ngroups counters,
-// zero on entry and zero again when the launch ends.  scratch: blockDim.x
+// red.partials: (nblocks + ngroups) * n doubles; red.count: 1 + ngroups
+// counters, zero on entry and zero again when the launch ends.  scratch: blockDim.x
 // doubles of shared memory.  The grid may be 2-D; blocks are numbered
 // x-fastest.
-__device__ __forceinline__ bool grid_reduce_last(const double *tot, int n, double *partials,
-                                                 unsigned int *count, double *out, double *scratch) {
+__device__ __forceinline__ bool grid_reduce_last(const double *tot, int n, const RedScratch &red, double *out,
+                                                 double *scratch) {
   __shared__ bool am_last;
   const int nb = gridDim.x * gridDim.y, bid = blockIdx.y * gridDim.x + blockIdx.x;
   const int ngroups = (nb + RED_GROUP - 1) / RED_GROUP, g = bid / RED_GROUP;
   const int gsize = min(RED_GROUP, nb - g * RED_GROUP);
+  // the host sizes the scratch first (ensure_red); a launch that would not
+  // fit writes nothing, flags the error and runs no finisher
+  if ((size_t)(nb + ngroups) * n > red.max_partials || (size_t)(1 + ngroups) > red.max_count) {
+    if (bid == 0 && threadIdx.x == 0) atomicExch(red.err, 1);
+    return false;
+  }
+  double *partials = red.partials;
+  unsigned int *count = red.count;
   double *grows = partials + (size_t)nb * n;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) partials[(size_t)bid * n + i] = tot[i];
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) am_last = (atomicAdd(&count[1 + g], 1u) == (unsigned)gsize - 1);
+  // one thread writes the block's row, publishes it (fence) and arrives, so
+  // a single fence per block orders every store the arrival covers
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < n; i++) partials[(size_t)bid * n + i] = tot[i];
+    __threadfence();
+    am_last = (atomicAdd(&count[1 + g], 1u) == (unsigned)gsize - 1);
+  }
   __syncthreads();
   if (!am_last) return false;
   __threadfence();
-  sum_rows(partials + (size_t)g * RED_GROUP * n, gsize, n, grows + (size_t)g * n, scratch);
-  __threadfence();
-  __syncthreads();
+  sum_rows(partials + (size_t)g * RED_GROUP * n, gsize, n, out, scratch);  // out: shared staging
   if (threadIdx.x == 0) {
+    for (int i = 0; i < n; i++) grows[(size_t)g * n + i] = out[i];
     count[1 + g] = 0;  // every block of the group has arrived
+    __threadfence();
     am_last = (atomicAdd(&count[0], 1u) == (unsigned)ngroups - 1);
   }
   __syncthreads();

@@ -323,9 +323,9 @@ static int launch_site(int family, const Op &op, const Fin &fin, const int *skip
   int gx = grid_for(Vh, 256);
   int cap = c.sm_count * 4;
   if (gx > cap) gx = cap;
-  MKS_TRY(ensure_red(NSUM > 0 ? NSUM * nsrc : 1, gx));
+  MKS_TRY(ensure_red(NSUM > 0 ? NSUM * nsrc : 1, gx * nsrc));  // one row per block of the (gx, nsrc) grid
   timing_begin(family);
-  k_site<Op, NSUM, Fin><<<dim3(gx, nsrc), 256, 0, c.stream>>>(op, fin, skip, Vh, c.red.partials, c.red.count,
+  k_site<Op, NSUM, Fin><<<dim3(gx, nsrc), 256, 0, c.stream>>>(op, fin, skip, Vh, c.red,
                                                              totals);
   timing_end(family);
   MKS_CUDA(cudaGetLastError());
@@ -376,8 +376,7 @@ static int launch_dslash_nb(int family, const LinkT &fat, const LinkT &lng,
   int grid = (int)((threads + block - 1) / block);
   if (NSUM > 0) {
     MKS_TRY(ensure_red(NSUM * a.groups * NB, grid));
-    a.partials = c.red.partials;
-    a.count = c.red.count;
+    a.red = c.red;
   }
   timing_begin(family);
   k_dslash<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin><<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
@@ -647,7 +646,7 @@ static int read_states(Solver &S, int nsrc, CgState *h) {
   Context &c = ctx();
   MKS_CUDA(cudaMemcpyAsync(h, S.st, nsrc * sizeof(CgState), cudaMemcpyDeviceToHost, c.stream));
   MKS_CUDA(cudaStreamSynchronize(c.stream));
-  return MKS_OK;
+  return red_check();
 }
 static int write_states(Solver &S, int nsrc, const CgState *h, int skip) {
   Context &c = ctx();

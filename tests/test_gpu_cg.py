@@ -81,6 +81,24 @@ def test_block_cg_each_source_matches_single(gpu, oracle_cls, prec, nsrc):
         assert rel(xs[k], xo) < 1e-7, (k, rel(xs[k], xo))
 
 
+@pytest.mark.parametrize("prec", ["PREC_SINGLE", "PREC_HALF"])
+def test_block_cg_16_sources_larger_lattice(gpu, oracle_cls, prec):
+    """16 sources on 16^4: reduction grids with thousands of blocks and
+    16-row BLAS launches (multi-level reduction, scratch sizing)."""
+    m = gpu
+    dims = (16, 16, 16, 16)
+    orc, fat, lng = _setup(m, oracle_cls, dims)
+    srcs = [m.gen_vector(dims, 300 + k, m.EVEN) for k in range(16)]
+    xs = [np.zeros_like(s) for s in srcs]
+    qic = m.QuarkInvertControl(resid=1e-10, max=2000, nrestart=5, parity=m.EVEN, prec=getattr(m, prec))
+    it, per = m.ks_congrad_block_parity(srcs, xs, qic, 0.05)
+    assert it > 10
+    assert all(p.converged == 1 for p in per)
+    for k in (0, 7, 15):
+        _, xo, _ = orc.congrad(fat, lng, srcs[k], np.zeros_like(srcs[k]), 0.05, m.EVEN, 1e-13, 0.0, 2000, 5)
+        assert rel(xs[k], xo) < 1e-7, (k, rel(xs[k], xo))
+
+
 @pytest.mark.parametrize("prec", ["PREC_DOUBLE", "PREC_SINGLE"])
 def test_mat_invert_uml_matches_oracle(gpu, oracle_cls, prec):
     m = gpu
