@@ -200,6 +200,12 @@ int mks_get_hisq_aux(double *V, double *W);
    generic_ks/su3_mat_op.c:1037-1080) would have switched to its SVD branch;
    the analytic projection was used for them.  Returns a count >= 0. */
 int mks_hisq_reunit_svd_count(void);
+/* Rebuild the fat/long links of slots 0..n_naiks-1 from the thin links
+ * already resident on the device (after mks_update_u / mks_reunitarize or
+ * mks_gauge_load): restore_fermion_links_from_site after
+ * invalidate_fermion_links (generic_ks/fermion_links_hisq_milc.c,
+ * ks_imp_rhmc/update_u.c:66).  Same arguments as mks_load_links_from_thin. */
+int mks_rebuild_links(int action, int n_naiks, const double *eps_naik, double u0);
 
 /* Generic-coefficient loaders, one per MILC GPU loader:
  * coeffs = {one_link, naik, three_staple, five_staple, seven_staple, lepage}
@@ -270,7 +276,8 @@ int mks_force_filter_count(void);
 #define MKS_K_LINKS        6
 #define MKS_K_FORCE        7
 #define MKS_K_TUNE         8   /* autotuner trial launches */
-#define MKS_K_COUNT        9
+#define MKS_K_GAUGE        9   /* gauge force/action, link update, momenta, RNG */
+#define MKS_K_COUNT        10
 int mks_timing_enable(int on);
 int mks_timing_reset(void);
 int mks_timing_get(int family, double *total_ms, long long *launches);
@@ -294,6 +301,48 @@ int mks_bench_dslash(int prec, int nsrc, int parity, int slot, int iters, int fl
  * launched (environment MKS_TUNE=0 keeps a fixed table).  Returns
  * MKS_ERR_STATE when the pair has not been launched yet. */
 int mks_tuned_shape(int prec, int nsrc, int *G, int *nb, int *block);
+
+/* ------------------------------------------------------------------ */
+/* Gauge side of the RHMC molecular dynamics (mks_gauge.cu).  The library
+ * keeps one resident thin-link field (the one the fermion links are built
+ * from; phases in on the device) and one momentum field, and updates them
+ * in place, as MILC's lattice[].link / lattice[].mom.  Changing the thin
+ * links invalidates every fermion-link slot (mks_rebuild_links rebuilds).
+ *  - mks_gauge_load / mks_gauge_get: thin links WITHOUT phases, host
+ *    double[V][4][18] (MILC's rephase(OFF) state).
+ *  - mks_mom_load / mks_mom_get: anti_hermitmat[V][4].
+ *  - mks_rng_seed: MILC's site generators (SITERAND), seeded like
+ *    initialize_site_prn_from_seed (generic/ranstuff.c:117-130) from iseed
+ *    and each site's lexicographic index; mks_ranmom replaces ranmom
+ *    (generic/ranmom.c); mks_gaussian_vector draws three complex Gaussians
+ *    per site of `parity` into v (other sites untouched), as grsource_rhmc.c:
+ *    31-41 does.  The streams continue from call to call.
+ *  - mks_gauge_force replaces imp_gauge_force_ks / imp_gauge_force_gpu
+ *    (generic_ks/gauge_force_imp_ks.c, generic/gauge_force_imp.c:37-223):
+ *    mom <- TA(mom - eps beta/3 U sum c staples) for MILC's HISQ-improved
+ *    Symanzik action (plaquette, rectangle, bent loop;
+ *    generic/imp_actions/symanzik_1loop_hisq_action.h; nflavors = the
+ *    total_dyn_flavors of make_loop_table).
+ *  - mks_gauge_action: (beta/3) imp_gauge_action (generic/gauge_stuff.c:277),
+ *    the g term of d_action_rhmc.c:27-29.
+ *  - mks_update_u replaces update_u (ks_imp_rhmc/update_u.c:49-108):
+ *    U <- exp(eps mom) U to eighth order.
+ *  - mks_mom_action: hmom_action (ks_imp_rhmc/d_action_rhmc.c:89-122).
+ *  - mks_reunitarize: reunitarize_ks (generic_ks/reunitarize_ks.c).
+ *  - mks_plaquette: d_plaquette (generic/d_plaq4.c) without phases. */
+int mks_gauge_load(const double *thin);
+int mks_gauge_get(double *thin);
+int mks_mom_load(const double *mom);
+int mks_mom_get(double *mom);
+int mks_rng_seed(int iseed);
+int mks_ranmom(void);
+int mks_gaussian_vector(int parity, double *v);
+int mks_gauge_force(double eps, double beta, double u0, int nflavors);
+int mks_gauge_action(double beta, double u0, int nflavors, double *action);
+int mks_update_u(double eps);
+int mks_mom_action(double *h);
+int mks_reunitarize(void);
+int mks_plaquette(double *ss, double *st);
 
 /* ------------------------------------------------------------------ */
 /* Host-side synthetic inputs (no device work).  See mks_fields.c. */

@@ -34,7 +34,9 @@ __all__ = ["EVEN", "ODD", "EVENANDODD", "PREC_HALF", "PREC_SINGLE", "PREC_DOUBLE
            "ks_congrad_field",
            "ks_congrad_block_parity", "mat_invert_uml_field", "mat_invert_block_uml",
            "ks_multicg_offset_field", "ks_ratinv", "ks_rateval", "load_hisq_links", "load_asqtad_links", "get_hisq_aux",
-           "eo_fermion_force_multi", "fermion_force_adjoint", "gen_thin_links", "apply_phases", "gen_vector", "gen_momenta",
+           "eo_fermion_force_multi", "fermion_force_adjoint", "gauge_load", "gauge_get", "mom_load", "mom_get",
+           "rng_seed", "ranmom", "gaussian_vector", "gauge_force", "gauge_action", "update_u", "mom_action",
+           "reunitarize", "plaquette", "rebuild_links", "gen_thin_links", "apply_phases", "gen_vector", "gen_momenta",
            "MksError"]
 
 
@@ -242,6 +244,81 @@ def fermion_force_adjoint(residues, xxx, n_orders_naik=None, n_naiks=1):
     check(init().mks_fermion_force_adjoint(_dp(res), _pp(list(xxx)), len(res), ords, n_naiks, _dp(ku)),
           "mks_fermion_force_adjoint")
     return ku
+
+
+# ---- gauge side of the RHMC: resident thin links and momenta ----
+def gauge_load(thin_unphased):
+    """Resident thin links from MILC's host layout without phases."""
+    check(init().mks_gauge_load(_dp(np.ascontiguousarray(thin_unphased, dtype=np.float64))), "mks_gauge_load")
+
+
+def gauge_get():
+    V = int(np.prod(_state["dims"]))
+    U = np.zeros((V, 4, 18))
+    check(init().mks_gauge_get(_dp(U)), "mks_gauge_get")
+    return U
+
+
+def mom_load(mom):
+    check(init().mks_mom_load(_dp(np.ascontiguousarray(mom, dtype=np.float64))), "mks_mom_load")
+
+
+def mom_get():
+    V = int(np.prod(_state["dims"]))
+    mom = np.zeros((V, 4, 10))
+    check(init().mks_mom_get(_dp(mom)), "mks_mom_get")
+    return mom
+
+
+def rng_seed(iseed):
+    check(init().mks_rng_seed(int(iseed)), "mks_rng_seed")
+
+
+def ranmom():
+    check(init().mks_ranmom(), "mks_ranmom")
+
+
+def gaussian_vector(parity, v=None):
+    V = int(np.prod(_state["dims"]))
+    v = np.zeros((V, 6)) if v is None else v
+    check(init().mks_gaussian_vector(parity, _dp(v)), "mks_gaussian_vector")
+    return v
+
+
+def gauge_force(eps, beta, u0, nflavors):
+    check(init().mks_gauge_force(eps, beta, u0, nflavors), "mks_gauge_force")
+
+
+def gauge_action(beta, u0, nflavors):
+    a = ctypes.c_double()
+    check(init().mks_gauge_action(beta, u0, nflavors, ctypes.byref(a)), "mks_gauge_action")
+    return a.value
+
+
+def update_u(eps):
+    check(init().mks_update_u(eps), "mks_update_u")
+
+
+def mom_action():
+    h = ctypes.c_double()
+    check(init().mks_mom_action(ctypes.byref(h)), "mks_mom_action")
+    return h.value
+
+
+def reunitarize():
+    check(init().mks_reunitarize(), "mks_reunitarize")
+
+
+def plaquette():
+    ss, st = ctypes.c_double(), ctypes.c_double()
+    check(init().mks_plaquette(ctypes.byref(ss), ctypes.byref(st)), "mks_plaquette")
+    return ss.value, st.value
+
+
+def rebuild_links(action="hisq", eps_naik=(0.0,), u0=1.0):
+    eps = np.ascontiguousarray(eps_naik, dtype=np.float64)
+    act = _lib.MKS_ACTION_HISQ if action == "hisq" else _lib.MKS_ACTION_ASQTAD
+    check(init().mks_rebuild_links(act, len(eps), _dp(eps), u0), "mks_rebuild_links")
 
 
 # ---- host-side synthetic inputs (no device work) ----

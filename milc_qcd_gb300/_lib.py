@@ -15,7 +15,7 @@ MKS_PREC_HALF, MKS_PREC_SINGLE, MKS_PREC_DOUBLE = 0, 1, 2
 MKS_ACTION_HISQ, MKS_ACTION_ASQTAD = 1, 2
 MKS_MAX_SLOTS = 12
 KERNEL_FAMILIES = {"dslash_f64": 0, "dslash_f32": 1, "dslash_f16": 2, "dslash_mrhs": 3, "blas": 4,
-                   "shift": 5, "links": 6, "force": 7, "tune": 8}
+                   "shift": 5, "links": 6, "force": 7, "tune": 8, "gauge": 9}
 
 
 class InvertArg(ctypes.Structure):
@@ -78,6 +78,20 @@ SIGNATURES = {
     "mks_fermion_force_multi_asqtad": (ctypes.c_int, [ctypes.c_double, DP, DPP, ctypes.c_int, DP]),
     "mks_fermion_force_adjoint": (ctypes.c_int, [DP, DPP, ctypes.c_int, IP, ctypes.c_int, DP]),
     "mks_force_flops_last": (ctypes.c_double, []),
+    "mks_rebuild_links": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, DP, ctypes.c_double]),
+    "mks_gauge_load": (ctypes.c_int, [DP]),
+    "mks_gauge_get": (ctypes.c_int, [DP]),
+    "mks_mom_load": (ctypes.c_int, [DP]),
+    "mks_mom_get": (ctypes.c_int, [DP]),
+    "mks_rng_seed": (ctypes.c_int, [ctypes.c_int]),
+    "mks_ranmom": (ctypes.c_int, []),
+    "mks_gaussian_vector": (ctypes.c_int, [ctypes.c_int, DP]),
+    "mks_gauge_force": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int]),
+    "mks_gauge_action": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.c_int, DP]),
+    "mks_update_u": (ctypes.c_int, [ctypes.c_double]),
+    "mks_mom_action": (ctypes.c_int, [DP]),
+    "mks_reunitarize": (ctypes.c_int, []),
+    "mks_plaquette": (ctypes.c_int, [DP, DP]),
     "mks_force_filter_count": (ctypes.c_int, []),
     "mks_timing_enable": (ctypes.c_int, [ctypes.c_int]),
     "mks_timing_reset": (ctypes.c_int, []),

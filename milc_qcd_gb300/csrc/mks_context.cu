@@ -380,6 +380,10 @@ static void free_lattice_fields() {
   ws_free_all();
   dev_free(c.auxU); dev_free(c.auxV); dev_free(c.auxW);
   c.auxU = c.auxV = c.auxW = nullptr;
+  c.aux_action = 0;
+  dev_free(c.mom);
+  c.mom = nullptr;
+  gauge_free();
 }
 
 int mks_finalize(void) {

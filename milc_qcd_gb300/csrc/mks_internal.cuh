@@ -275,6 +275,26 @@ struct RedScratch {
 };
 int red_check();  // MKS_ERR_CUDA (and clears the flag) if a reduction overran
 
+// gauge side of the molecular dynamics (mks_gauge.cu), on the resident
+// thin links and momenta
+void gauge_free();
+int gauge_force_dev(double eps, double beta, double u0, int nflavors);
+int gauge_action_dev(double beta, double u0, int nflavors, double *action);
+int mom_action_dev(double *h);
+int plaquette_dev(double *ss, double *st);
+int update_u_dev(double eps);
+int reunitarize_dev();
+int ranmom_dev();
+int gauss_vec_dev(int parity, double *v_dev);
+int norm2_aos_dev(const double *v_dev, int par, double *out);
+int lincomb_aos_dev(int par, const double *src, const double *const *x, const double *a, int n, double *out);
+int prn_seed_dev(int seed);
+// fat/long links of slots 0..n_naiks-1 from the resident thin links (mks_links.cu)
+int links_from_aux(int action, int n_naiks, const double *eps_naik, double u0);
+// fermion force on device SoA solution fields (mks_force.cu)
+int force_dev(double eps, const double *residues, double2 *const *xs, int nterms, const int *orders, int n_naiks,
+              double *mom_dev, double2 *ku_out);
+
 // ------------------------------------------------------------------
 // host-side context
 struct LinkSlot {
@@ -304,6 +324,8 @@ struct Context {
   double2 *auxU = nullptr, *auxV = nullptr, *auxW = nullptr;
   int aux_action = 0;
   double aux_u0 = 1.0;
+  // gauge momenta of the molecular dynamics (anti_hermitmat[V][4], device)
+  double *mom = nullptr;
   // timing
   bool timing = false;
   double kernel_ms[MKS_K_COUNT] = {0};

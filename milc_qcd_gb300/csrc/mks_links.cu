@@ -186,16 +186,24 @@ static unsigned int g_nsvd = 0;
 
 int links_from_thin(int action, const double *thin_dev_aos, int n_naiks, const double *eps_naik, double u0) {
   Context &c = ctx();
-  size_t Vh = c.Vh, nall = 8 * 9 * Vh;
+  size_t nall = 8 * 9 * c.Vh;
   if (!c.auxU) {
     MKS_TRY(dev_alloc((void **)&c.auxU, nall * sizeof(double2)));
     MKS_TRY(dev_alloc((void **)&c.auxV, nall * sizeof(double2)));
     MKS_TRY(dev_alloc((void **)&c.auxW, nall * sizeof(double2)));
   }
+  MKS_TRY(links_aos_to_soa64(thin_dev_aos, c.auxU));
+  return links_from_aux(action, n_naiks, eps_naik, u0);
+}
+
+// fat/long links of slots 0..n_naiks-1 built from the resident thin links auxU
+int links_from_aux(int action, int n_naiks, const double *eps_naik, double u0) {
+  Context &c = ctx();
+  size_t Vh = c.Vh, nall = 8 * 9 * Vh;
+  if (!c.auxU) return MKS_ERR_STATE;
   double2 *staple, *tmp, *f3 = nullptr, *l3 = nullptr;
   MKS_TRY(dev_alloc((void **)&staple, 2 * 9 * Vh * sizeof(double2)));
   MKS_TRY(dev_alloc((void **)&tmp, 2 * 9 * Vh * sizeof(double2)));
-  MKS_TRY(links_aos_to_soa64(thin_dev_aos, c.auxU));
   for (int i = 0; i < n_naiks; i++) {
     LinkSlot &s = c.slots[i];
     if (!s.fat64) {
@@ -274,6 +282,14 @@ int mks_load_links_from_thin(int action, const double *thin, int n_naiks, const 
   cudaStreamSynchronize(c.stream);
   dev_free(tmp);
   return rc;
+}
+
+int mks_rebuild_links(int action, int n_naiks, const double *eps_naik, double u0) {
+  MKS_TRY(check_ready());
+  if (action != MKS_ACTION_HISQ && action != MKS_ACTION_ASQTAD) return MKS_ERR_ARG;
+  if (n_naiks < 1 || n_naiks > MKS_MAX_SLOTS || (n_naiks > 1 && !eps_naik) || !(u0 > 0)) return MKS_ERR_ARG;
+  if (!ctx().auxU) return MKS_ERR_STATE;
+  return links_from_aux(action, n_naiks, eps_naik, u0);
 }
 
 int mks_hisq_reunit_svd_count(void) { return (int)g_nsvd; }

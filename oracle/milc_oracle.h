@@ -14,6 +14,7 @@
 #ifndef MILC_ORACLE_H
 #define MILC_ORACLE_H
 #include <stddef.h>
+#include <stdint.h>
 
 #define ORC_ODD 0x01
 #define ORC_EVEN 0x02
@@ -71,4 +72,37 @@ void orc_fermion_force_hisq(const orc_lat *L, const double *U, int n_naiks,
 double orc_force_action(const orc_lat *L, const double *U, int n_naiks, const double *eps_naik,
                         const double *residues, const double *xxx, int nterms,
                         const int *n_orders_naik);
+
+/* ---- gauge side of the RHMC (milc_oracle_gauge.c) ---- */
+#define ORC_MAX_LOOPS 16     /* orientations per loop kind (gauge_stuff.c MAX_NUM) */
+#define ORC_MAX_STAPLES 64   /* staple paths per link direction */
+typedef struct {
+  int nloop;
+  int length[3];
+  int num[3];
+  int dirs[3][ORC_MAX_LOOPS][6];
+  double coeff[3];
+} orc_loops;
+
+typedef struct {
+  uint32_t r[7];
+  uint64_t multiplier, addend, ic_state;
+} orc_prn;
+
+void orc_loop_table(int nflavors, double u0, orc_loops *T);
+double orc_gauge_action(const orc_lat *L, const double *U, double beta, double u0, int nflavors);
+void orc_gauge_force(const orc_lat *L, const double *U, double eps, double beta, double u0, int nflavors,
+                     double *mom);
+void orc_update_u(const orc_lat *L, double *U, const double *mom, double eps);
+double orc_hmom_action(const orc_lat *L, const double *mom);
+void orc_reunitarize(const orc_lat *L, double *U);
+void orc_plaquette(const orc_lat *L, const double *U, double *ss, double *st);
+void orc_prn_init(orc_prn *p, int seed, int index);
+double orc_myrand(orc_prn *p);
+double orc_gaussian(orc_prn *p);
+void orc_complex_gaussian(orc_prn *p, double *re, double *im);
+void orc_site_prn_init(const orc_lat *L, int seed, orc_prn *prn);
+void orc_ranmom(const orc_lat *L, orc_prn *prn, double *mom);
+void orc_gaussian_vector(const orc_lat *L, orc_prn *prn, int parity, double *v);
+
 #endif

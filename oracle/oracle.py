@@ -181,6 +181,78 @@ class Oracle:
                                          ords.ctypes.data_as(_ip))
 
 
+class _Prn(ctypes.Structure):
+    _fields_ = [("r", ctypes.c_uint32 * 7), ("multiplier", ctypes.c_uint64), ("addend", ctypes.c_uint64),
+                ("ic_state", ctypes.c_uint64)]
+
+
+class _Loops(ctypes.Structure):
+    _fields_ = [("nloop", ctypes.c_int), ("length", ctypes.c_int * 3), ("num", ctypes.c_int * 3),
+                ("dirs", ((ctypes.c_int * 6) * 16) * 3), ("coeff", ctypes.c_double * 3)]
+
+
+class GaugeOracle:
+    """Gauge side of the RHMC (milc_oracle_gauge.c) on one Oracle's geometry.
+    Links are unphased, momenta (V, 4, 10); the site random generators are
+    held here (MILC's SITERAND streams)."""
+
+    def __init__(self, orc):
+        self.orc, self.lib, self.L, self.V = orc, orc.lib, orc.L, orc.V
+        lib = self.lib
+        lib.orc_gauge_action.restype = ctypes.c_double
+        lib.orc_hmom_action.restype = ctypes.c_double
+        lib.orc_myrand.restype = ctypes.c_double
+        lib.orc_gaussian.restype = ctypes.c_double
+        self.prn = None
+
+    def loop_table(self, nflavors, u0):
+        T = _Loops()
+        self.lib.orc_loop_table(ctypes.c_int(nflavors), ctypes.c_double(u0), ctypes.byref(T))
+        return T
+
+    def action(self, U, beta, u0, nflavors):
+        return self.lib.orc_gauge_action(self.L, _ptr(U), ctypes.c_double(beta), ctypes.c_double(u0),
+                                         ctypes.c_int(nflavors))
+
+    def force(self, U, eps, beta, u0, nflavors, mom):
+        mom = mom.copy()
+        self.lib.orc_gauge_force(self.L, _ptr(U), ctypes.c_double(eps), ctypes.c_double(beta),
+                                 ctypes.c_double(u0), ctypes.c_int(nflavors), _ptr(mom))
+        return mom
+
+    def update_u(self, U, mom, eps):
+        U = U.copy()
+        self.lib.orc_update_u(self.L, _ptr(U), _ptr(mom), ctypes.c_double(eps))
+        return U
+
+    def hmom_action(self, mom):
+        return self.lib.orc_hmom_action(self.L, _ptr(mom))
+
+    def reunitarize(self, U):
+        U = U.copy()
+        self.lib.orc_reunitarize(self.L, _ptr(U))
+        return U
+
+    def plaquette(self, U):
+        ss, st = ctypes.c_double(), ctypes.c_double()
+        self.lib.orc_plaquette(self.L, _ptr(U), ctypes.byref(ss), ctypes.byref(st))
+        return ss.value, st.value
+
+    def seed(self, iseed):
+        self.prn = (_Prn * self.V)()
+        self.lib.orc_site_prn_init(self.L, ctypes.c_int(iseed), self.prn)
+
+    def ranmom(self):
+        mom = np.zeros((self.V, 4, 10))
+        self.lib.orc_ranmom(self.L, self.prn, _ptr(mom))
+        return mom
+
+    def gaussian_vector(self, parity):
+        v = np.zeros((self.V, 6))
+        self.lib.orc_gaussian_vector(self.L, self.prn, ctypes.c_int(parity), _ptr(v))
+        return v
+
+
 class MilcRef:
     """MILC's own CPU implementation (single lattice per process)."""
 
@@ -263,6 +335,48 @@ class MilcRef:
                                          ctypes.c_int(max_iter), ctypes.c_int(nrestart),
                                          ctypes.c_int(inaik), _ptr(frsq))
         return it, psim, frsq
+
+    # ---- gauge side of the RHMC (MILC's own routines) ----
+    def set_gauge_params(self, beta, u0, dyn_flavors):
+        fl = (ctypes.c_int * len(dyn_flavors))(*dyn_flavors)
+        self.lib.ref_set_gauge_params(ctypes.c_double(beta), ctypes.c_double(u0), ctypes.c_int(len(dyn_flavors)), fl)
+
+    def gauge_action(self):
+        self.lib.ref_gauge_action.restype = ctypes.c_double
+        return self.lib.ref_gauge_action()
+
+    def gauge_force(self, eps, mom):
+        mom = np.ascontiguousarray(mom, dtype=np.float64).copy()
+        self.lib.ref_gauge_force(ctypes.c_double(eps), _ptr(mom))
+        return mom
+
+    def update_u(self, eps, mom):
+        self.lib.ref_update_u(ctypes.c_double(eps), _ptr(np.ascontiguousarray(mom, dtype=np.float64)))
+
+    def hmom_action(self, mom):
+        self.lib.ref_hmom_action.restype = ctypes.c_double
+        return self.lib.ref_hmom_action(_ptr(np.ascontiguousarray(mom, dtype=np.float64)))
+
+    def seed(self, iseed):
+        self.lib.ref_seed(ctypes.c_int(iseed))
+
+    def ranmom(self):
+        mom = np.zeros((self.V, 4, 10))
+        self.lib.ref_ranmom(_ptr(mom))
+        return mom
+
+    def gaussian_vector(self, parity):
+        v = np.zeros((self.V, 6))
+        self.lib.ref_gaussian_vector(ctypes.c_int(parity), _ptr(v))
+        return v
+
+    def reunitarize(self):
+        self.lib.ref_reunitarize()
+
+    def plaquette(self):
+        ss, st = ctypes.c_double(), ctypes.c_double()
+        self.lib.ref_plaquette(ctypes.byref(ss), ctypes.byref(st))
+        return ss.value, st.value
 
     def fermion_force(self, eps, residues, xxx, orders=None, mom=None):
         res = np.ascontiguousarray(residues, dtype=np.float64)

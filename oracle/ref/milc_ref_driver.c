@@ -285,3 +285,85 @@ void ref_fermion_force(double eps, const double *residues, const double *xxx,
 }
 
 int ref_sizeof_anti_hermitmat(void) { return (int)sizeof(anti_hermitmat); }
+
+/* ---------------- gauge side of the RHMC ----------------
+ * MILC's own routines, called as ks_imp_rhmc's update() calls them:
+ *   make_loop_table / imp_gauge_action   generic/gauge_stuff.c:87,277
+ *   imp_gauge_force_ks                   generic_ks/gauge_force_imp_ks.c:8
+ *   update_u                             ks_imp_rhmc/update_u.c:49
+ *   hmom_action                          ks_imp_rhmc/d_action_rhmc.c:89
+ *   ranmom / site generators             generic/ranmom.c, generic/ranstuff.c:117
+ *   reunitarize_ks                       generic_ks/reunitarize_ks.c:9
+ *   d_plaquette                          generic/d_plaq4.c
+ * Links pass through ref_set_thin_links / ref_get_thin_links_phased;
+ * momenta are anti_hermitmat[4*i+dir]. */
+static int ref_loops_made = 0;
+
+void ref_set_gauge_params(double b, double u0v, int nmasses, const int *flavors) {
+  int i;
+  beta = b;
+  u0 = u0v;
+  n_dyn_masses = nmasses;
+  for (i = 0; i < nmasses; i++) dyn_flavors[i] = flavors[i];
+  if (!ref_loops_made) { make_loop_table(); ref_loops_made = 1; }
+}
+
+static void ref_put_mom(const double *mom) {
+  size_t i;
+  for (i = 0; i < sites_on_node; i++) memcpy(&lattice[i].mom[0], mom + i * 40, 4 * sizeof(anti_hermitmat));
+}
+static void ref_take_mom(double *mom) {
+  size_t i;
+  for (i = 0; i < sites_on_node; i++) memcpy(mom + i * 40, &lattice[i].mom[0], 4 * sizeof(anti_hermitmat));
+}
+
+double ref_gauge_action(void) {
+  double g;
+  rephase(OFF);
+  g = (beta / 3.0) * imp_gauge_action();
+  rephase(ON);
+  return g;
+}
+
+void ref_gauge_force(double eps, double *mom) {
+  ref_put_mom(mom);
+  imp_gauge_force_ks(eps, F_OFFSET(mom));
+  ref_take_mom(mom);
+}
+
+void ref_update_u(double eps, const double *mom) {
+  ref_put_mom(mom);
+  update_u(eps);
+}
+
+double ref_hmom_action(const double *mom) {
+  ref_put_mom(mom);
+  return hmom_action();
+}
+
+void ref_seed(int seed) {
+  iseed = seed;
+  initialize_site_prn_from_seed(seed);
+}
+
+void ref_ranmom(double *mom) {
+  ranmom();
+  ref_take_mom(mom);
+}
+
+/* three complex Gaussians per site of `parity`, as grsource_rhmc.c:31-41 */
+void ref_gaussian_vector(int parity, double *v) {
+  int i, j;
+  site *s;
+  FORSOMEPARITY(i, s, parity) {
+    for (j = 0; j < 3; j++) {
+      complex z = complex_gaussian_rand_no(&(s->site_prn));
+      v[6 * i + 2 * j] = z.real;
+      v[6 * i + 2 * j + 1] = z.imag;
+    }
+  }
+}
+
+void ref_reunitarize(void) { reunitarize_ks(); }
+
+void ref_plaquette(double *ss, double *st) { d_plaquette(ss, st); }
