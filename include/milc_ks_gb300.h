@@ -345,6 +345,62 @@ int mks_reunitarize(void);
 int mks_plaquette(double *ss, double *st);
 
 /* ------------------------------------------------------------------ */
+/* One RHMC molecular-dynamics trajectory (mks_rhmc.cu): MILC's update()
+ * (ks_imp_rhmc/update_rhmc.c:182-473) for the HISQ action on the resident
+ * thin links and momenta.  With refresh = 1 it draws the momenta (ranmom)
+ * and one heat-bath source per pseudofermion field (grsource_rhmc.c:
+ * phi = R_GR(M^dag M) g, g Gaussian on even sites) from the site
+ * generators (mks_rng_seed first); with refresh = 0 it reuses the momenta
+ * and the fields of the previous call.  It computes the action
+ * (d_action_rhmc.c: g, h, f), integrates `steps` steps of size `epsilon`
+ * with the chosen integrator, and the action again; the links and momenta
+ * are left at the trajectory's end (the caller accepts or restores them;
+ * MILC draws its Metropolis number from node_prn).  Multi-shift solves use
+ * the offsets pole[1..order] and the residues res[0..order] of each
+ * rational function (MILC's rationals file, ks_imp_rhmc/
+ * load_rhmc_params.c), with resid_* NOT squared (cgresid_md_fa_gr) and
+ * prec_* the inner precision (FP64 reproduces MILC's double build). */
+#define MKS_INT_LEAPFROG 0
+#define MKS_INT_OMELYAN  1
+#define MKS_INT_2G1F     2
+#define MKS_INT_3G1F     3
+#define MKS_RHMC_MAX_PSEUDO 16
+typedef struct {
+  int order;            /* number of poles */
+  const double *res;    /* order+1 residues, res[0] the constant term */
+  const double *pole;   /* order+1 poles, pole[0] unused */
+} mks_ratfunc;
+typedef struct {
+  double naik_eps;      /* naik_term_epsilon of the field (first field: 0) */
+  mks_ratfunc md, gr, fa;
+  double resid_md, resid_fa, resid_gr;
+  int max_cg;           /* max_multicg_md_fa_gr */
+} mks_pseudofermion;
+typedef struct {
+  double beta, u0;      /* gauge coupling and tadpole factor of the gauge action */
+  int nflavors;         /* total_dyn_flavors (gauge action coefficients) */
+  double epsilon;       /* microcanonical_time_step */
+  int steps;            /* steps_per_trajectory */
+  int int_alg;          /* MKS_INT_* */
+  int n_pseudo;
+  const mks_pseudofermion *pf;
+  int prec_md, prec_fa, prec_gr;  /* MKS_PREC_* */
+  int nrestart;         /* CG restarts (MILC's nrestart, 0 -> 5) */
+  int refresh;
+} mks_rhmc_params;
+typedef struct {
+  double g0, h0, f0;    /* action terms at the start */
+  double g1, h1, f1;    /* and at the end of the trajectory */
+  double delta_s;       /* (g1+h1+f1) - (g0+h0+f0) */
+  double plaq_ss, plaq_st;  /* plaquettes at the end (no phases) */
+  double grsource_sum[MKS_RHMC_MAX_PSEUDO];  /* |g|^2 of each heat-bath Gaussian */
+  long long cg_iters;   /* summed multi-shift iterations */
+  int n_solves, unconverged, n_gauge_force, n_fermion_force;
+  double t_total, t_solve, t_fermion_force, t_gauge_force, t_links;  /* seconds */
+} mks_rhmc_result;
+int mks_rhmc_trajectory(const mks_rhmc_params *p, mks_rhmc_result *r);
+
+/* ------------------------------------------------------------------ */
 /* Host-side synthetic inputs (no device work).  See mks_fields.c. */
 void   mks_site_coords(const int dims[4], size_t index, int xyzt[4]);
 size_t mks_site_index(const int dims[4], const int xyzt[4]);

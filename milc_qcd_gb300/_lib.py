@@ -79,6 +79,7 @@ SIGNATURES = {
     "mks_fermion_force_adjoint": (ctypes.c_int, [DP, DPP, ctypes.c_int, IP, ctypes.c_int, DP]),
     "mks_force_flops_last": (ctypes.c_double, []),
     "mks_rebuild_links": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, DP, ctypes.c_double]),
+    "mks_rhmc_trajectory": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "mks_gauge_load": (ctypes.c_int, [DP]),
     "mks_gauge_get": (ctypes.c_int, [DP]),
     "mks_mom_load": (ctypes.c_int, [DP]),
@@ -128,6 +129,39 @@ def load(path=LIB_PATH):
         fn.argtypes = args
     _lib = lib
     return lib
+
+
+MKS_INT_LEAPFROG, MKS_INT_OMELYAN, MKS_INT_2G1F, MKS_INT_3G1F = 0, 1, 2, 3
+MKS_RHMC_MAX_PSEUDO = 16
+
+
+class RatFunc(ctypes.Structure):
+    _fields_ = [("order", ctypes.c_int), ("res", DP), ("pole", DP)]
+
+
+class Pseudofermion(ctypes.Structure):
+    _fields_ = [("naik_eps", ctypes.c_double), ("md", RatFunc), ("gr", RatFunc), ("fa", RatFunc),
+                ("resid_md", ctypes.c_double), ("resid_fa", ctypes.c_double), ("resid_gr", ctypes.c_double),
+                ("max_cg", ctypes.c_int)]
+
+
+class RhmcParams(ctypes.Structure):
+    _fields_ = [("beta", ctypes.c_double), ("u0", ctypes.c_double), ("nflavors", ctypes.c_int),
+                ("epsilon", ctypes.c_double), ("steps", ctypes.c_int), ("int_alg", ctypes.c_int),
+                ("n_pseudo", ctypes.c_int), ("pf", ctypes.POINTER(Pseudofermion)),
+                ("prec_md", ctypes.c_int), ("prec_fa", ctypes.c_int), ("prec_gr", ctypes.c_int),
+                ("nrestart", ctypes.c_int), ("refresh", ctypes.c_int)]
+
+
+class RhmcResult(ctypes.Structure):
+    _fields_ = [("g0", ctypes.c_double), ("h0", ctypes.c_double), ("f0", ctypes.c_double),
+                ("g1", ctypes.c_double), ("h1", ctypes.c_double), ("f1", ctypes.c_double),
+                ("delta_s", ctypes.c_double), ("plaq_ss", ctypes.c_double), ("plaq_st", ctypes.c_double),
+                ("grsource_sum", ctypes.c_double * MKS_RHMC_MAX_PSEUDO), ("cg_iters", ctypes.c_longlong),
+                ("n_solves", ctypes.c_int), ("unconverged", ctypes.c_int), ("n_gauge_force", ctypes.c_int),
+                ("n_fermion_force", ctypes.c_int), ("t_total", ctypes.c_double), ("t_solve", ctypes.c_double),
+                ("t_fermion_force", ctypes.c_double), ("t_gauge_force", ctypes.c_double),
+                ("t_links", ctypes.c_double)]
 
 
 class MksError(RuntimeError):

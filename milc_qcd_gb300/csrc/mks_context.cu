@@ -384,6 +384,7 @@ static void free_lattice_fields() {
   dev_free(c.mom);
   c.mom = nullptr;
   gauge_free();
+  rhmc_free();
 }
 
 int mks_finalize(void) {

@@ -88,3 +88,51 @@ def parse_rhmc_params(text, n_pseudo=None):
 def load_rhmc_params(path, n_pseudo=None):
     with open(path) as f:
         return parse_rhmc_params(f.read(), n_pseudo)
+
+
+# ---- one trajectory on the GPU (mks_rhmc_trajectory) ----
+INTEGRATORS = {"leapfrog": 0, "omelyan": 1, "2G1F": 2, "3G1F": 3}
+
+
+def update(pseudofermions, beta, u0, nflavors, epsilon, steps, int_alg="3G1F", resid_md=None, resid_fa=None,
+           resid_gr=None, max_cg=2500, prec_md=2, prec_fa=2, prec_gr=2, nrestart=5, refresh=True):
+    """MILC's update() (ks_imp_rhmc/update_rhmc.c) on the resident links and
+    momenta.  pseudofermions: list of PseudofermionParams (or dicts with
+    'MD'/'GR'/'FA' -> (res, pole) and 'naik_term_epsilon'); resid_*: one
+    residual per field (cgresid_md_fa_gr, not squared).  Returns a dict of
+    the action terms, delta_s, plaquettes, counters and timings."""
+    import ctypes
+    import numpy as np
+    from . import _lib, init, check
+
+    n = len(pseudofermions)
+    keep = []
+
+    def ratf(fn):
+        if isinstance(fn, RationalFunction):
+            res, pole = fn.res, fn.pole
+        else:
+            res, pole = fn
+        res = np.ascontiguousarray(res, dtype=np.float64)
+        pole = np.ascontiguousarray(pole, dtype=np.float64)
+        keep.extend([res, pole])
+        return _lib.RatFunc(len(res) - 1, res.ctypes.data_as(_lib.DP), pole.ctypes.data_as(_lib.DP))
+
+    arr = (_lib.Pseudofermion * n)()
+    for i, pf in enumerate(pseudofermions):
+        if isinstance(pf, PseudofermionParams):
+            eps, md, gr, fa = pf.naik_term_epsilon, pf.MD, pf.GR, pf.FA
+        else:
+            eps, md, gr, fa = pf.get("naik_term_epsilon", 0.0), pf["MD"], pf["GR"], pf["FA"]
+        arr[i] = _lib.Pseudofermion(float(eps), ratf(md), ratf(gr), ratf(fa), resid_md[i], resid_fa[i],
+                                    resid_gr[i], int(max_cg))
+    p = _lib.RhmcParams(beta, u0, int(nflavors), epsilon, int(steps), INTEGRATORS[int_alg], n,
+                        ctypes.cast(arr, ctypes.POINTER(_lib.Pseudofermion)), prec_md, prec_fa, prec_gr,
+                        int(nrestart), 1 if refresh else 0)
+    r = _lib.RhmcResult()
+    check(init().mks_rhmc_trajectory(ctypes.byref(p), ctypes.byref(r)), "mks_rhmc_trajectory")
+    out = {f: getattr(r, f) for f, _ in _lib.RhmcResult._fields_ if f != "grsource_sum"}
+    out["grsource_sum"] = [r.grsource_sum[i] for i in range(n)]
+    out["start"] = (r.g0, r.h0, r.f0)
+    out["end"] = (r.g1, r.h1, r.f1)
+    return out
