@@ -237,5 +237,90 @@ void eo_fermion_force_twoterms(Real eps, Real weight1, Real weight2, su3_vector 
 /* Host allocators named by MILC's -DUSE_FL_GPU code paths (see
    mks_milc_alloc.h).  Plain malloc: the library copies from pageable memory
    correctly, pinning only changes the copy speed. */
+#ifdef USE_GF_GPU
+/* ---- gauge side of the molecular dynamics (-DUSE_GF_GPU) ----
+ * Replaces imp_gauge_force_gpu (generic/gauge_force_imp_gpu.c:15),
+ * reunitarize_gpu (generic/reunitarize2.c:210) and the QUDA variant of
+ * update_u (ks_imp_rhmc/update_u.c:23-45; drop update_u.o, this file
+ * defines update_u).  MILC keeps links and momenta in its site structure,
+ * so each call uploads them (links without phases), runs the kernel and
+ * copies back what changed; a trajectory that stays on the GPU from start
+ * to end is mks_rhmc_trajectory. */
+static double *mks_links_buf = NULL, *mks_mom_buf = NULL;
+
+static void mks_put_links(void) {
+  int i, dir, k, st;
+  site *s;
+  if (!mks_links_buf) mks_links_buf = (double *)malloc(sizeof(double) * 72 * sites_on_node);
+  FORALLSITES(i, s) for (dir = XUP; dir <= TUP; dir++) {
+    const double *m = (const double *)&s->link[dir];
+    double ph = (phases_in == ON) ? s->phase[dir] : 1.0;   /* phases are +-1 */
+    for (k = 0; k < 18; k++) mks_links_buf[(4 * i + dir) * 18 + k] = ph * m[k];
+  }
+  if ((st = mks_gauge_load(mks_links_buf)) < 0) mks_die("mks_gauge_load", st);
+}
+
+static void mks_take_links(void) {
+  int i, dir, k, st;
+  site *s;
+  if ((st = mks_gauge_get(mks_links_buf)) < 0) mks_die("mks_gauge_get", st);
+  FORALLSITES(i, s) for (dir = XUP; dir <= TUP; dir++) {
+    double *m = (double *)&s->link[dir];
+    double ph = (phases_in == ON) ? s->phase[dir] : 1.0;
+    for (k = 0; k < 18; k++) m[k] = ph * mks_links_buf[(4 * i + dir) * 18 + k];
+  }
+}
+
+static void mks_put_mom(field_offset mom_off) {
+  int i, st;
+  site *s;
+  if (!mks_mom_buf) mks_mom_buf = (double *)malloc(sizeof(double) * 40 * sites_on_node);
+  FORALLSITES(i, s) memcpy(mks_mom_buf + 40 * i, F_PT(s, mom_off), 4 * sizeof(anti_hermitmat));
+  if ((st = mks_mom_load(mks_mom_buf)) < 0) mks_die("mks_mom_load", st);
+}
+
+static void mks_take_mom(field_offset mom_off) {
+  int i, st;
+  site *s;
+  if ((st = mks_mom_get(mks_mom_buf)) < 0) mks_die("mks_mom_get", st);
+  FORALLSITES(i, s) memcpy(F_PT(s, mom_off), mks_mom_buf + 40 * i, 4 * sizeof(anti_hermitmat));
+}
+
+static int mks_total_flavors(void) {
+  int i, n = 0;
+  for (i = 0; i < n_dyn_masses; i++) n += dyn_flavors[i];
+  return n;
+}
+
+void imp_gauge_force_gpu(Real eps, field_offset mom_off) {
+  int st;
+  mks_setup();
+  mks_put_links();
+  mks_put_mom(mom_off);
+  if ((st = mks_gauge_force(eps, beta, u0, mks_total_flavors())) < 0) mks_die("imp_gauge_force_gpu", st);
+  mks_take_mom(mom_off);
+}
+
+void update_u(Real eps) {
+  int st;
+#ifdef FN
+  invalidate_fermion_links(fn_links);
+#endif
+  mks_setup();
+  mks_put_links();
+  mks_put_mom(F_OFFSET(mom));
+  if ((st = mks_update_u(eps)) < 0) mks_die("update_u", st);
+  mks_take_links();
+}
+
+void reunitarize_gpu(void) {
+  int st;
+  mks_setup();
+  mks_put_links();
+  if ((st = mks_reunitarize()) < 0) mks_die("reunitarize_gpu", st);
+  mks_take_links();
+}
+#endif /* USE_GF_GPU */
+
 void *qudaAllocatePinned(size_t bytes) { return malloc(bytes); }
 void qudaFreePinned(void *ptr) { free(ptr); }

@@ -26,6 +26,12 @@ def _inc(tmp_path):
             "-I" + os.path.join(ROOT, "include")]
 
 
+def test_glue_compiles_with_gpu_gauge_side(tmp_path):
+    src = os.path.join(ROOT, "milc_qcd_gb300", "milc_glue", "mks_milc_glue.c")
+    r = subprocess.run(["gcc"] + FLAGS + ["-DUSE_GF_GPU"] + _inc(tmp_path) + [src], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+
+
 @pytest.mark.parametrize("src", [
     os.path.join(ROOT, "milc_qcd_gb300", "milc_glue", "mks_milc_glue.c"),
     REF + "/generic_ks/fermion_links_hisq_load_milc.c",
