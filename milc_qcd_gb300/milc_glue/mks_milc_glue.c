@@ -196,6 +196,7 @@ void load_hisq_aux_links_gpu(info_t *info, ks_action_paths_hisq *ap, hisq_auxili
   info->final_flop = 61632. * volume / numnodes();
 }
 
+#if FERM_ACTION == HISQ
 /* generic_ks/fermion_force_hisq_multi.c:170-219: mom[dir] += TA(+-2 eps U dS/dU) */
 void eo_fermion_force_multi(Real eps, Real *residues, su3_vector **xxx, int nterms, int prec,
                             fermion_links_t *fl) {
@@ -220,6 +221,33 @@ void eo_fermion_force_multi(Real eps, Real *residues, su3_vector **xxx, int nter
   FORALLSITES(i, s) { memcpy(s->mom, mom + 40 * i, 4 * sizeof(anti_hermitmat)); }
   free(mom); free(res); free(orders);
 }
+#else
+/* asqtad: generic_ks/fermion_force_multi.c:29-44 (FNMAT,
+   fermion_force_fn_multi.c:80-316); the links are rebuilt on the device from
+   the thin links (phases in) with MILC's tadpole factor u0 */
+void eo_fermion_force_multi(Real eps, Real *residues, su3_vector **xxx, int nterms, int prec,
+                            fermion_links_t *fl) {
+  double *mom = (double *)malloc(sites_on_node * 4 * sizeof(anti_hermitmat));
+  double *thin = (double *)malloc(sites_on_node * 72 * sizeof(double));
+  double *res = (double *)malloc(nterms * sizeof(double));
+  double eps0 = 0.0;
+  int i, dir, st;
+  site *s;
+  (void)prec; (void)fl;
+  mks_setup();
+  for (i = 0; i < nterms; i++) res[i] = residues[i];
+  FORALLSITES(i, s) {
+    memcpy(mom + 40 * i, s->mom, 4 * sizeof(anti_hermitmat));
+    for (dir = XUP; dir <= TUP; dir++) memcpy(thin + (4 * i + dir) * 18, &s->link[dir], 18 * sizeof(double));
+  }
+  if ((st = mks_load_links_from_thin(MKS_ACTION_ASQTAD, thin, 1, &eps0, u0)) < 0)
+    mks_die("eo_fermion_force_multi", st);
+  st = mks_fermion_force_multi_asqtad(eps, res, (const double *const *)xxx, nterms, mom);
+  if (st < 0) mks_die("eo_fermion_force_multi", st);
+  FORALLSITES(i, s) { memcpy(s->mom, mom + 40 * i, 4 * sizeof(anti_hermitmat)); }
+  free(mom); free(thin); free(res);
+}
+#endif
 
 void eo_fermion_force_oneterm(Real eps, Real weight, su3_vector *temp_x, int prec, fermion_links_t *fl) {
   su3_vector *xxx[1] = {temp_x};

@@ -26,6 +26,16 @@ def _inc(tmp_path):
             "-I" + os.path.join(ROOT, "include")]
 
 
+def test_glue_compiles_for_asqtad(tmp_path):
+    src = os.path.join(ROOT, "milc_qcd_gb300", "milc_glue", "mks_milc_glue.c")
+    inc = _inc(tmp_path)
+    (tmp_path / "inc" / "quark_action.h").write_text('#include "%s/generic_ks/imp_actions/asqtad_action.h"\n' % REF)
+    (tmp_path / "inc" / "gauge_action.h").write_text('#include "%s/generic/imp_actions/symanzik_1loop_action.h"\n' % REF)
+    flags = [f for f in FLAGS if f != "-DHISQ_FF_MULTI_WRAPPER"]
+    r = subprocess.run(["gcc"] + flags + ["-DUSE_GF_GPU"] + inc + [src], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+
+
 def test_glue_compiles_with_gpu_gauge_side(tmp_path):
     src = os.path.join(ROOT, "milc_qcd_gb300", "milc_glue", "mks_milc_glue.c")
     r = subprocess.run(["gcc"] + FLAGS + ["-DUSE_GF_GPU"] + _inc(tmp_path) + [src], capture_output=True, text=True)
