@@ -132,6 +132,14 @@ def cpu_baseline(sample_iters=20, threads=None):
             "link_build_s": t_links}
 
 
+# dram__bytes_read.sum + dram__bytes_write.sum per launch of the multi-source
+# D_eo family (mean of the plain D and the fused CG-epilogue launch), from
+# one ncu capture of this benchmark on GB300 (4 launches of each kernel)
+MEASURED_TRAFFIC = {
+    ("single", 8, (32, 32, 32, 64)): 0.5 * (1.776e9 + 2.278e9),
+    ("single", 4, (32, 32, 32, 64)): 0.5 * (1.520e9 + 1.722e9),
+}
+
 # FP64 CG iterations to |r|/|b| = 1e-10 on this workload (32^3x64, m = 0.01,
 # seeded links and source): MILC's CG and the GPU FP64 arm take the same
 # count (identical recurrences), measured by the GPU arm on GB300.
@@ -226,7 +234,40 @@ def extras(m, lib, _lib, torch, srcs):
     dt = time.time() - t0
     out["hisq_force_16c32_6terms"] = {"s_per_call": dt, "gflops_fp64": lib.mks_force_flops_last() / dt / 1e9,
                                       "includes": "host<->device copies of 6 vectors and the momenta"}
+    out["rhmc_trajectory"] = rhmc_trajectory(m, RHMC_DIMS)
     m.set_lattice(DIMS)
+    return out
+
+
+# HISQ RHMC trajectory: MILC's 2+1 regression set-up (4 pseudofermion
+# fields, the rational functions of MILC's sample rationals file, 3G1F,
+# 10 steps of 0.02) on a larger seeded lattice, once with FP32 multi-shift
+# solves (the production setting) and once with FP64 solves from the same
+# start, for Delta H against the FP64 run
+RHMC_DIMS = (16, 16, 16, 32)
+
+
+def rhmc_trajectory(m, dims, seed=5):
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import rhmc_sample as R
+    from milc_qcd_gb300.rhmc import update
+    d = R.load()
+    pfs = [dict(d["rational"][i], naik_term_epsilon=float(d["naik_eps"][i])) for i in range(R.N_PSEUDO)]
+    m.set_lattice(dims)
+    V = int(np.prod(dims))
+    U0 = m.gen_thin_links(dims, seed, 0.2)
+    out = {"lattice": list(dims), "pseudofermions": R.N_PSEUDO, "integrator": "3G1F", "steps": R.STEPS,
+           "epsilon": R.EPSILON, "masses": [0.0018, 0.018], "rationals": "MILC sample (2+1, 4 fields)"}
+    for name, prec in (("f32", m.PREC_SINGLE), ("f64", m.PREC_DOUBLE)):
+        m.gauge_load(U0)
+        m.mom_load(np.zeros((V, 4, 10)))
+        m.rng_seed(seed)
+        r = update(pfs, R.BETA, R.U0, R.nflavors(), R.EPSILON, R.STEPS, R.INT_ALG, R.RESID_MD, R.RESID_FA,
+                   R.RESID_GR, R.MAX_CG, prec, prec, prec, R.NRESTART, True)
+        out[name] = {"s_per_trajectory": r["t_total"], "delta_h": r["delta_s"], "cg_iters": r["cg_iters"],
+                     "t_solve": r["t_solve"], "t_fermion_force": r["t_fermion_force"],
+                     "t_gauge_force": r["t_gauge_force"], "t_links": r["t_links"], "unconverged": r["unconverged"]}
+    out["delta_h_f32_minus_f64"] = out["f32"]["delta_h"] - out["f64"]["delta_h"]
     return out
 
 
@@ -331,6 +372,7 @@ def gpu_arm(args):
     else:
         per_site = 16 * 18 * 8 + N * 0.5 * ((48 + 48) + (48 + 48 + 48 + 48))
     alg_bytes = per_site * Vh
+    traffic = MEASURED_TRAFFIC.get((args.prec, N, tuple(DIMS)))
     peak, peak_kind = peaks()
     achieved = alg_bytes / (dslash_ms * 1e-3) / 1e9
     # plain FP64 D_eo and FP32 D_eo standalone timings (L2 flushed between launches)
@@ -373,7 +415,8 @@ def gpu_arm(args):
         "dslash_gbs": {"f32_single_rhs": gbs32, "f32_ms": ms32.value, "f64_ms": ms64.value,
                        "f64_gflops": 1146.0 * Vh / (ms64.value * 1e-3) / 1e9},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": "k_dslash (%s, nsrc=%d)" % (args.prec, N),
+                     "traffic": traffic, "traffic_unit": "bytes per launch (mean of the D and D+epilogue launches)",
+                     "kernel": "k_dslash (%s, nsrc=%d)" % (args.prec, N),
                      "peak_source": peak_kind, "avg_launch_ms": dslash_ms, "launches": nl.value},
         "e2e": {"value": e2e_per_src, "unit": "s/solve", "h2d_bytes_per_step": 2 * N * bytes_field,
                 "d2h_bytes_per_step": N * bytes_field},

@@ -80,6 +80,21 @@ k_dslash(const LinkT fat, const LinkT lng, const DslashArgs<InT, OutT, typename 
 #pragma unroll
     for (int k = 0; k < (NSUM > 0 ? NSUM : 1); k++) sums[s][k] = R(0);
 
+#ifndef MKS_EPI_PREFETCH
+#define MKS_EPI_PREFETCH 0
+#endif
+  if (MKS_EPI_PREFETCH && EPI == EPI_AXPY && grp == 0 && (h & 15) == 0 && h < Vh) {
+    // the epilogue operands are needed only after the 16 neighbour terms:
+    // start bringing them into L2 now (one thread per 16 sites)
+#pragma unroll
+    for (int s = 0; s < NB; s++) {
+      const int S = grp * NB + s;
+      if (S < a.nsrc) {
+        a.p[S].prefetch16(h, Vh);
+        if (NSUM >= 3) a.r[S].prefetch16(h, Vh);
+      }
+    }
+  }
   if (h < Vh) {
     int x, y, z, t;
     site_coords(g, par, h, x, y, z, t);

@@ -120,8 +120,23 @@ __device__ __forceinline__ int wrap_add(int c, int k, int n) {
 
 // ------------------------------------------------------------------
 // field accessors
+
+// ask L2 for the 128-byte line holding address a (a hint: no register is
+// held and nothing is returned)
+__device__ __forceinline__ void prefetch_l2(const void *a) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+}
+
 struct VecF64 {
   double2 *p;  // [3][Vh]
+  // lines of the 16 sites h..h+15 (h a multiple of 16)
+  __device__ __forceinline__ void prefetch16(int h, int Vh) const {
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      prefetch_l2(p + (size_t)c * Vh + h);
+      if (h + 8 < Vh) prefetch_l2(p + (size_t)c * Vh + h + 8);
+    }
+  }
   __device__ __forceinline__ V3<double> load(int h, int Vh) const {
     V3<double> v;
 #pragma unroll
@@ -135,6 +150,11 @@ struct VecF64 {
 };
 struct VecF32 {
   float2 *p;  // [3][Vh]
+  // lines of the 16 sites h..h+15 (h a multiple of 16)
+  __device__ __forceinline__ void prefetch16(int h, int Vh) const {
+#pragma unroll
+    for (int c = 0; c < 3; c++) prefetch_l2(p + (size_t)c * Vh + h);
+  }
   __device__ __forceinline__ V3<float> load(int h, int Vh) const {
     V3<float> v;
 #pragma unroll
