@@ -81,7 +81,7 @@ k_dslash(const LinkT fat, const LinkT lng, const DslashArgs<InT, OutT, typename 
     for (int k = 0; k < (NSUM > 0 ? NSUM : 1); k++) sums[s][k] = R(0);
 
 #ifndef MKS_EPI_PREFETCH
-#define MKS_EPI_PREFETCH 0
+#define MKS_EPI_PREFETCH 1  // measured: 3 % faster 8-source CG on GB300
 #endif
   if (MKS_EPI_PREFETCH && EPI == EPI_AXPY && grp == 0 && (h & 15) == 0 && h < Vh) {
     // the epilogue operands are needed only after the 16 neighbour terms:

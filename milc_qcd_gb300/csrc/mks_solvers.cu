@@ -353,7 +353,8 @@ static LinkSet16 links16(const LinkSlot &s) {
 // turns tuning off (fixed table); the choices can be read back with
 // mks_tuned_shape().
 struct Shape { int G, NB, block; };
-static Shape g_shape[3][MAXSRC + 1];  // [prec][nsrc], G == 0: not chosen yet
+static Shape g_shape[3][MAXSRC + 1];      // [prec][nsrc], G == 0: not chosen yet
+static Shape g_shape_epi[3][MAXSRC + 1];  // the same for the fused-epilogue launches
 
 static Shape default_shape(int nsrc) {
   if (nsrc <= 1) return {1, 1, 256};
@@ -416,7 +417,9 @@ static void set_vec(VecF64 &v, float *p, float *) { v.p = (double2 *)p; }
 static void set_vec(VecF32 &v, float *p, float *) { v.p = (float2 *)p; }
 static void set_vec(VecF16 &v, float *p, float *n) { v.p = (__half2 *)p; v.norm = n; }
 
-template <class LinkT>
+// EPI = EPI_AXPY times the fused CG epilogue (3 sums, no finisher): its
+// block reduction and extra reads can favour another shape than plain D
+template <class LinkT, int EPI = EPI_PLAIN>
 static int tune_shape(const LinkT &fat, const LinkT &lng, int nsrc, Shape *best) {
   typedef PrecOf<LinkT> P;
   typedef typename P::R R;
@@ -439,6 +442,21 @@ static int tune_shape(const LinkT &fat, const LinkT &lng, int nsrc, Shape *best)
     k_fill_tune<<<c.sm_count * 4, 256, 0, c.stream>>>(nrm, c.Vh);
     set_vec(a.in[s], in, nrm);
     set_vec(a.out[s], out, nrm);
+    if (EPI == EPI_AXPY) {
+      float *pp, *rr;
+      MKS_TRY(wsv("tune_p" + std::to_string(s), n * 4, &pp));
+      MKS_TRY(wsv("tune_r" + std::to_string(s), n * 4, &rr));
+      k_fill_tune<<<c.sm_count * 4, 256, 0, c.stream>>>(pp, n * 4);
+      k_fill_tune<<<c.sm_count * 4, 256, 0, c.stream>>>(rr, n * 4);
+      a.p[s].p = (decltype(a.p[s].p))pp;
+      a.r[s].p = (decltype(a.r[s].p))rr;
+      a.coef[s] = -0.01;
+    }
+  }
+  if (EPI == EPI_AXPY) {
+    float *tot;
+    MKS_TRY(wsv("tune_totals", 2 * MAXSRC * 3, &tot));
+    a.totals = (double *)tot;
   }
   MKS_CUDA(cudaGetLastError());
   cudaEvent_t e0, e1;
@@ -455,7 +473,8 @@ static int tune_shape(const LinkT &fat, const LinkT &lng, int nsrc, Shape *best)
         float tot = 0;
         for (int it = 0; it < 4; it++) {
           MKS_CUDA(cudaEventRecord(e0, c.stream));
-          MKS_TRY((launch_shape<R, LinkT, InT, OutT, EPI_PLAIN, 0>(MKS_K_TUNE, fat, lng, a, NoFinish(), sh)));
+          MKS_TRY((launch_shape<R, LinkT, InT, OutT, EPI, (EPI == EPI_AXPY ? 3 : 0)>(MKS_K_TUNE, fat, lng, a,
+                                                                                      NoFinish(), sh)));
           MKS_CUDA(cudaEventRecord(e1, c.stream));
           MKS_CUDA(cudaEventSynchronize(e1));
           float ms;
@@ -498,10 +517,13 @@ template <typename R, class LinkT, class InT, class OutT, int EPI, int NSUM, cla
 static int launch_dslash(int family, const LinkT &fat, const LinkT &lng,
                          DslashArgs<InT, OutT, typename EpiLoad<R>::type> &a, const Fin &fin) {
   const int pk = PrecOf<LinkT>::v;
-  Shape &sh = g_shape[pk][a.nsrc];
+  Shape &sh = (EPI == EPI_AXPY ? g_shape_epi : g_shape)[pk][a.nsrc];
   if (sh.G == 0) {
     Shape t;
-    if (!shape_override(pk, a.nsrc, &t)) MKS_TRY(tune_shape(fat, lng, a.nsrc, &t));
+    if (!shape_override(pk, a.nsrc, &t)) {
+      if (EPI == EPI_AXPY) MKS_TRY((tune_shape<LinkT, EPI_AXPY>(fat, lng, a.nsrc, &t)));
+      else MKS_TRY(tune_shape(fat, lng, a.nsrc, &t));
+    }
     sh = t;
   }
   if (a.nsrc > 1 && family != MKS_K_DSLASH_F64) family = MKS_K_DSLASH_MRHS;
