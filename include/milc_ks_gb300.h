@@ -338,6 +338,9 @@ int mks_rng_seed(int iseed);
 int mks_ranmom(void);
 int mks_gaussian_vector(int parity, double *v);
 int mks_gauge_force(double eps, double beta, double u0, int nflavors);
+/* the same with the staple sums in `prec` (MKS_PREC_DOUBLE as above, or
+   MKS_PREC_SINGLE: FP32 staples and products, FP64 momentum update) */
+int mks_gauge_force_prec(double eps, double beta, double u0, int nflavors, int prec);
 int mks_gauge_action(double beta, double u0, int nflavors, double *action);
 int mks_update_u(double eps);
 int mks_mom_action(double *h);
@@ -387,6 +390,7 @@ typedef struct {
   int prec_md, prec_fa, prec_gr;  /* MKS_PREC_* */
   int nrestart;         /* CG restarts (MILC's nrestart, 0 -> 5) */
   int refresh;
+  int prec_gauge_force; /* MKS_PREC_DOUBLE (0 also means double) or MKS_PREC_SINGLE */
 } mks_rhmc_params;
 typedef struct {
   double g0, h0, f0;    /* action terms at the start */

@@ -285,8 +285,8 @@ def gaussian_vector(parity, v=None):
     return v
 
 
-def gauge_force(eps, beta, u0, nflavors):
-    check(init().mks_gauge_force(eps, beta, u0, nflavors), "mks_gauge_force")
+def gauge_force(eps, beta, u0, nflavors, prec=PREC_DOUBLE):
+    check(init().mks_gauge_force_prec(eps, beta, u0, nflavors, prec), "mks_gauge_force_prec")
 
 
 def gauge_action(beta, u0, nflavors):

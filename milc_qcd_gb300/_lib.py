@@ -89,6 +89,8 @@ SIGNATURES = {
     "mks_gaussian_vector": (ctypes.c_int, [ctypes.c_int, DP]),
     "mks_gauge_force": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int]),
     "mks_gauge_action": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.c_int, DP]),
+    "mks_gauge_force_prec": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                            ctypes.c_int]),
     "mks_update_u": (ctypes.c_int, [ctypes.c_double]),
     "mks_mom_action": (ctypes.c_int, [DP]),
     "mks_reunitarize": (ctypes.c_int, []),
@@ -150,7 +152,7 @@ class RhmcParams(ctypes.Structure):
                 ("epsilon", ctypes.c_double), ("steps", ctypes.c_int), ("int_alg", ctypes.c_int),
                 ("n_pseudo", ctypes.c_int), ("pf", ctypes.POINTER(Pseudofermion)),
                 ("prec_md", ctypes.c_int), ("prec_fa", ctypes.c_int), ("prec_gr", ctypes.c_int),
-                ("nrestart", ctypes.c_int), ("refresh", ctypes.c_int)]
+                ("nrestart", ctypes.c_int), ("refresh", ctypes.c_int), ("prec_gauge_force", ctypes.c_int)]
 
 
 class RhmcResult(ctypes.Structure):

@@ -205,48 +205,101 @@ static int upload_paths(int nflavors, double u0) {
   return MKS_OK;
 }
 
-// product of the links along `path` from site c (modified: ends at the path's end)
-__device__ __forceinline__ M3<double> walk(const Geom &g, const double2 *U, int c[4], const signed char *path,
-                                           int len) {
-  const int L[4] = {g.nx, g.ny, g.nz, g.nt};
-  M3<double> P;
+template <typename R>
+__device__ __forceinline__ M3<R> to_r(const M3<double> &m) {
+  M3<R> o;
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
-    for (int j = 0; j < 3; j++) P.e[i][j] = {i == j ? 1.0 : 0.0, 0.0};
+    for (int j = 0; j < 3; j++) o.e[i][j] = {(R)m.e[i][j].re, (R)m.e[i][j].im};
+  return o;
+}
+template <typename R>
+__device__ __forceinline__ M3<R> mul_nn(const M3<R> &a, const M3<R> &b) {
+  M3<R> c;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      R re = 0, im = 0;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        re = fma(a.e[i][k].re, b.e[k][j].re, re); re = fma(-a.e[i][k].im, b.e[k][j].im, re);
+        im = fma(a.e[i][k].re, b.e[k][j].im, im); im = fma(a.e[i][k].im, b.e[k][j].re, im);
+      }
+      c.e[i][j] = {re, im};
+    }
+  return c;
+}
+template <typename R>
+__device__ __forceinline__ M3<R> mul_na(const M3<R> &a, const M3<R> &b) {  // a b^dag
+  M3<R> c;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      R re = 0, im = 0;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        re = fma(a.e[i][k].re, b.e[j][k].re, re); re = fma(a.e[i][k].im, b.e[j][k].im, re);
+        im = fma(a.e[i][k].im, b.e[j][k].re, im); im = fma(-a.e[i][k].re, b.e[j][k].im, im);
+      }
+      c.e[i][j] = {re, im};
+    }
+  return c;
+}
+
+// product of the links along `path` from site c (modified: ends at the
+// path's end), in arithmetic R (links stored FP64)
+template <typename R>
+__device__ __forceinline__ M3<R> walk_r(const Geom &g, const double2 *U, int c[4], const signed char *path, int len) {
+  const int L[4] = {g.nx, g.ny, g.nz, g.nt};
+  M3<R> P;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) P.e[i][j] = {i == j ? (R)1 : (R)0, (R)0};
   for (int k = 0; k < len; k++) {
     const int d = path[k];
     if (d < 4) {
-      P = mm_nn(P, load_link(g, U, c, d, true));
+      P = mul_nn<R>(P, to_r<R>(load_link(g, U, c, d, true)));
       c[d] = wrap_add(c[d], 1, L[d]);
     } else {
       const int dd = 7 - d;
       c[dd] = wrap_add(c[dd], -1, L[dd]);
-      P = mm_na(P, load_link(g, U, c, dd, true));
+      P = mul_na<R>(P, to_r<R>(load_link(g, U, c, dd, true)));
     }
   }
   return P;
 }
+__device__ __forceinline__ M3<double> walk(const Geom &g, const double2 *U, int c[4], const signed char *path,
+                                           int len) {
+  return walk_r<double>(g, U, c, path, len);
+}
 
 // mom_mu(x) <- TA(mom_mu(x) - eb3 U_mu(x) sum_p c_p Q_p), Q_p the staple
 // paths from x+mu back to x (links without phases)
+// staple sum and product in arithmetic R (FP64 reproduces MILC's double
+// build; FP32 runs at the FP32 rate for large-lattice molecular dynamics);
+// the momentum update is FP64 either way
+template <typename R>
 __global__ void __launch_bounds__(128) k_gauge_force(Geom g, const double2 *U, double *mom, double eb3) {
   const int h = blockIdx.x * blockDim.x + threadIdx.x, par = blockIdx.y, mu = blockIdx.z;
   if (h >= g.Vh) return;
   int x0[4];
   site_coords(g, par, h, x0[0], x0[1], x0[2], x0[3]);
   const int L[4] = {g.nx, g.ny, g.nz, g.nt};
-  M3<double> S;
+  M3<R> S;
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
-    for (int j = 0; j < 3; j++) S.e[i][j] = {0.0, 0.0};
+    for (int j = 0; j < 3; j++) S.e[i][j] = {(R)0, (R)0};
   const int np = c_staples.n[mu];
   for (int p = 0; p < np; p++) {
     int c[4] = {x0[0], x0[1], x0[2], x0[3]};
     c[mu] = wrap_add(c[mu], 1, L[mu]);
-    const M3<double> Q = walk(g, U, c, c_staples.dir[mu][p], c_staples.len[mu][p]);
-    const double cf = c_staples.c[mu][p];
+    const M3<R> Q = walk_r<R>(g, U, c, c_staples.dir[mu][p], c_staples.len[mu][p]);
+    const R cf = (R)c_staples.c[mu][p];
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -255,7 +308,12 @@ __global__ void __launch_bounds__(128) k_gauge_force(Geom g, const double2 *U, d
         S.e[i][j].im = fma(cf, Q.e[i][j].im, S.e[i][j].im);
       }
   }
-  const M3<double> G = mm_nn(load_link(g, U, x0, mu, true), S);
+  const M3<R> Gr = mul_nn<R>(to_r<R>(load_link(g, U, x0, mu, true)), S);
+  M3<double> G;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) G.e[i][j] = {(double)Gr.e[i][j].re, (double)Gr.e[i][j].im};
   double *m = mom + (((size_t)par * g.Vh + h) * 4 + mu) * 10;
   // A = uncompressed mom - eb3 G, then its traceless anti-Hermitian part
   // (libraries/uncmp_ahmat.c, make_ahmat.c)
@@ -601,11 +659,14 @@ static void thin_changed() {
 
 static dim3 link_grid() { return dim3(grid_for(ctx().Vh, 128), 2, 4); }
 
-int gauge_force_dev(double eps, double beta, double u0, int nflavors) {
+int gauge_force_dev(double eps, double beta, double u0, int nflavors, int prec) {
   Context &c = ctx();
   MKS_TRY(upload_paths(nflavors, u0));
   timing_begin(MKS_K_GAUGE);
-  k_gauge_force<<<link_grid(), 128, 0, c.stream>>>(c.geom, c.auxU, c.mom, eps * beta / 3.0);
+  if (prec == MKS_PREC_DOUBLE)
+    k_gauge_force<double><<<link_grid(), 128, 0, c.stream>>>(c.geom, c.auxU, c.mom, eps * beta / 3.0);
+  else
+    k_gauge_force<float><<<link_grid(), 128, 0, c.stream>>>(c.geom, c.auxU, c.mom, eps * beta / 3.0);
   timing_end(MKS_K_GAUGE);
   MKS_CUDA(cudaGetLastError());
   return MKS_OK;
@@ -818,10 +879,15 @@ int mks_gaussian_vector(int parity, double *v) {
 }
 
 int mks_gauge_force(double eps, double beta, double u0, int nflavors) {
+  return mks_gauge_force_prec(eps, beta, u0, nflavors, MKS_PREC_DOUBLE);
+}
+
+int mks_gauge_force_prec(double eps, double beta, double u0, int nflavors, int prec) {
   MKS_TRY(check_ready());
+  if (prec != MKS_PREC_DOUBLE && prec != MKS_PREC_SINGLE) return MKS_ERR_ARG;
   if (!ctx().auxU) return MKS_ERR_STATE;
   MKS_TRY(ensure_mom());
-  return gauge_force_dev(eps, beta, u0, nflavors);
+  return gauge_force_dev(eps, beta, u0, nflavors, prec);
 }
 
 int mks_gauge_action(double beta, double u0, int nflavors, double *action) {

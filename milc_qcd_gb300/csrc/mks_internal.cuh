@@ -299,7 +299,7 @@ int red_check();  // MKS_ERR_CUDA (and clears the flag) if a reduction overran
 // thin links and momenta
 void gauge_free();
 void rhmc_free();
-int gauge_force_dev(double eps, double beta, double u0, int nflavors);
+int gauge_force_dev(double eps, double beta, double u0, int nflavors, int prec);
 int gauge_action_dev(double beta, double u0, int nflavors, double *action);
 int mom_action_dev(double *h);
 int plaquette_dev(double *ss, double *st);

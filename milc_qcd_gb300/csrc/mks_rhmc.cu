@@ -132,7 +132,8 @@ struct Traj {
 
   int update_h_gauge(double eps) {
     const double t0 = wall();
-    MKS_TRY(gauge_force_dev(eps, p->beta, p->u0, p->nflavors));
+    MKS_TRY(gauge_force_dev(eps, p->beta, p->u0, p->nflavors,
+                            p->prec_gauge_force == MKS_PREC_SINGLE ? MKS_PREC_SINGLE : MKS_PREC_DOUBLE));
     MKS_CUDA(cudaStreamSynchronize(ctx().stream));
     r->t_gauge_force += wall() - t0;
     r->n_gauge_force++;

@@ -55,6 +55,14 @@ def test_gauge_force(setup):
     assert rel(m.mom_get(), G.force(U, 0.017, BETA, U0, NF, mom)) < 1e-14
 
 
+def test_gauge_force_fp32(setup):
+    m, U, mom, orc, G = setup
+    _load(m, U, mom)
+    m.gauge_force(0.017, BETA, U0, NF, m.PREC_SINGLE)
+    want = G.force(U, 0.017, BETA, U0, NF, mom)
+    assert rel(m.mom_get() - mom, want - mom) < 1e-5
+
+
 def test_update_u_and_reunitarize(setup):
     m, U, mom, orc, G = setup
     _load(m, U, mom)
