@@ -242,7 +242,7 @@ def extras(m, lib, _lib, torch, srcs):
 # HISQ RHMC trajectory: MILC's 2+1 regression set-up (4 pseudofermion
 # fields, the rational functions of MILC's sample rationals file, 3G1F,
 # 10 steps of 0.02) on a larger seeded lattice, once with FP32 multi-shift
-# solves and FP32 gauge-force staples (the production setting) and once all
+# solves and FP32 force arithmetic (the production setting) and once all
 # FP64 from the same start, for Delta H against the FP64 run
 RHMC_DIMS = (16, 16, 16, 32)
 
@@ -263,7 +263,7 @@ def rhmc_trajectory(m, dims, seed=5):
         m.mom_load(np.zeros((V, 4, 10)))
         m.rng_seed(seed)
         r = update(pfs, R.BETA, R.U0, R.nflavors(), R.EPSILON, R.STEPS, R.INT_ALG, R.RESID_MD, R.RESID_FA,
-                   R.RESID_GR, R.MAX_CG, prec, prec, prec, R.NRESTART, True, prec_gauge_force=prec)
+                   R.RESID_GR, R.MAX_CG, prec, prec, prec, R.NRESTART, True, prec_force=prec)
         out[name] = {"s_per_trajectory": r["t_total"], "delta_h": r["delta_s"], "cg_iters": r["cg_iters"],
                      "t_solve": r["t_solve"], "t_fermion_force": r["t_fermion_force"],
                      "t_gauge_force": r["t_gauge_force"], "t_links": r["t_links"], "unconverged": r["unconverged"]}

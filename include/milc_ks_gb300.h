@@ -346,6 +346,12 @@ int mks_update_u(double eps);
 int mks_mom_action(double *h);
 int mks_reunitarize(void);
 int mks_plaquette(double *ss, double *st);
+/* Arithmetic of the staple products in later link constructions
+ * (mks_load_links_from_thin, mks_rebuild_links) and fermion forces:
+ * MKS_PREC_DOUBLE (the default, MILC's double build) or MKS_PREC_SINGLE
+ * (FP32 products, FP64 fields and accumulation; for molecular-dynamics
+ * forces).  No reference counterpart: MILC's CPU force is FP64. */
+int mks_md_precision(int prec);
 
 /* ------------------------------------------------------------------ */
 /* One RHMC molecular-dynamics trajectory (mks_rhmc.cu): MILC's update()
@@ -390,7 +396,9 @@ typedef struct {
   int prec_md, prec_fa, prec_gr;  /* MKS_PREC_* */
   int nrestart;         /* CG restarts (MILC's nrestart, 0 -> 5) */
   int refresh;
-  int prec_gauge_force; /* MKS_PREC_DOUBLE (0 also means double) or MKS_PREC_SINGLE */
+  int prec_force;       /* arithmetic of the gauge force, the fermion force and the
+                           link rebuilds inside the integration: MKS_PREC_SINGLE, or
+                           FP64 (any other value); the action is always FP64 */
 } mks_rhmc_params;
 typedef struct {
   double g0, h0, f0;    /* action terms at the start */

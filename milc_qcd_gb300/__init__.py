@@ -36,7 +36,7 @@ __all__ = ["EVEN", "ODD", "EVENANDODD", "PREC_HALF", "PREC_SINGLE", "PREC_DOUBLE
            "ks_multicg_offset_field", "ks_ratinv", "ks_rateval", "load_hisq_links", "load_asqtad_links", "get_hisq_aux",
            "eo_fermion_force_multi", "fermion_force_adjoint", "gauge_load", "gauge_get", "mom_load", "mom_get",
            "rng_seed", "ranmom", "gaussian_vector", "gauge_force", "gauge_action", "update_u", "mom_action",
-           "reunitarize", "plaquette", "rebuild_links", "gen_thin_links", "apply_phases", "gen_vector", "gen_momenta",
+           "reunitarize", "plaquette", "rebuild_links", "md_precision", "gen_thin_links", "apply_phases", "gen_vector", "gen_momenta",
            "MksError"]
 
 
@@ -313,6 +313,10 @@ def plaquette():
     ss, st = ctypes.c_double(), ctypes.c_double()
     check(init().mks_plaquette(ctypes.byref(ss), ctypes.byref(st)), "mks_plaquette")
     return ss.value, st.value
+
+
+def md_precision(prec):
+    check(init().mks_md_precision(prec), "mks_md_precision")
 
 
 def rebuild_links(action="hisq", eps_naik=(0.0,), u0=1.0):

@@ -80,6 +80,7 @@ SIGNATURES = {
     "mks_force_flops_last": (ctypes.c_double, []),
     "mks_rebuild_links": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, DP, ctypes.c_double]),
     "mks_rhmc_trajectory": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "mks_md_precision": (ctypes.c_int, [ctypes.c_int]),
     "mks_gauge_load": (ctypes.c_int, [DP]),
     "mks_gauge_get": (ctypes.c_int, [DP]),
     "mks_mom_load": (ctypes.c_int, [DP]),
@@ -152,7 +153,7 @@ class RhmcParams(ctypes.Structure):
                 ("epsilon", ctypes.c_double), ("steps", ctypes.c_int), ("int_alg", ctypes.c_int),
                 ("n_pseudo", ctypes.c_int), ("pf", ctypes.POINTER(Pseudofermion)),
                 ("prec_md", ctypes.c_int), ("prec_fa", ctypes.c_int), ("prec_gr", ctypes.c_int),
-                ("nrestart", ctypes.c_int), ("refresh", ctypes.c_int), ("prec_gauge_force", ctypes.c_int)]
+                ("nrestart", ctypes.c_int), ("refresh", ctypes.c_int), ("prec_force", ctypes.c_int)]
 
 
 class RhmcResult(ctypes.Structure):

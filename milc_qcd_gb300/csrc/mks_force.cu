@@ -93,6 +93,7 @@ __global__ void __launch_bounds__(128) k_outer(Geom g, OuterArgs a, double2 *Kf,
 //   KA(y)    += U_nu(y-nu+mu)^dag K(y-nu) U_nu(y-nu) + U_nu(y+mu) K(y+nu) U_nu(y)^dag
 //   KUnu(y)  += A(y+nu) U_nu(y+mu)^dag K(y) + A(y-mu+nu)^dag U_nu(y-mu)^dag K(y-mu)^dag
 //             + K(y+nu)^dag U_nu(y+mu)^dag A(y)^dag + K(y+nu-mu) U_nu(y-mu)^dag A(y-mu)
+template <typename R>
 __global__ void __launch_bounds__(128) k_staple_adj(Geom g, int mu, int nu, MatF Unu, MatF A, MatF K, double f,
                                                     MatF KA, MatF KU) {
   const int h = blockIdx.x * blockDim.x + threadIdx.x;
@@ -102,34 +103,38 @@ __global__ void __launch_bounds__(128) k_staple_adj(Geom g, int mu, int nu, MatF
   const int ymnu = nbr(g, par, h, nu, -1), ypnu = nbr(g, par, h, nu, 1), ypmu = nbr(g, par, h, mu, 1);
   const int ymmu = nbr(g, par, h, mu, -1);
   const int ymnupmu = nbr2(g, par, h, nu, -1, mu, 1), ypnummu = nbr2(g, par, h, nu, 1, mu, -1);
-  const M3<double> Uy = Unu.ld(par, h, Vh);
-  const M3<double> Uypmu = Unu.ld(op, ypmu, Vh);
-  const M3<double> Uymmu = Unu.ld(op, ymmu, Vh);
+  const M3<R> Uy = narrow<R>(Unu.ld(par, h, Vh));
+  const M3<R> Uypmu = narrow<R>(Unu.ld(op, ypmu, Vh));
+  const M3<R> Uymmu = narrow<R>(Unu.ld(op, ymmu, Vh));
+  const R fr = (R)f;
   // KA
   {
-    M3<double> acc = KA.ld(par, h, Vh);
-    const M3<double> Uymnu = Unu.ld(op, ymnu, Vh);
-    const M3<double> Uymnupmu = Unu.ld(par, ymnupmu, Vh);
-    M3<double> t = mm_nn(mm_an(Uymnupmu, K.ld(op, ymnu, Vh)), Uymnu);
-    macc(acc, t, f);
-    t = mm_na(mm_nn(Uypmu, K.ld(op, ypnu, Vh)), Uy);
-    macc(acc, t, f);
-    KA.st(par, h, Vh, acc);
+    const M3<R> Uymnu = narrow<R>(Unu.ld(op, ymnu, Vh));
+    const M3<R> Uymnupmu = narrow<R>(Unu.ld(par, ymnupmu, Vh));
+    M3<R> acc = tnn<R>(tan_<R>(Uymnupmu, narrow<R>(K.ld(op, ymnu, Vh))), Uymnu);
+    const M3<R> t = tna<R>(tnn<R>(Uypmu, narrow<R>(K.ld(op, ypnu, Vh))), Uy);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) { acc.e[i][j].re += t.e[i][j].re; acc.e[i][j].im += t.e[i][j].im; }
+    M3<double> out = KA.ld(par, h, Vh);
+    macc(out, widen<R>(acc), f);
+    KA.st(par, h, Vh, out);
   }
   // KU_nu
   {
-    M3<double> acc = KU.ld(par, h, Vh);
-    const M3<double> Ky = K.ld(par, h, Vh), Ay = A.ld(par, h, Vh);
-    M3<double> t = mm_nn(mm_na(A.ld(op, ypnu, Vh), Uypmu), Ky);                       // T1
-    macc(acc, t, f);
-    t = adjm(mm_nn(K.ld(op, ymmu, Vh), mm_nn(Uymmu, A.ld(par, ypnummu, Vh))));         // T2 = (K U A)^dag
-    macc(acc, t, f);
-    t = adjm(mm_nn(Ay, mm_nn(Uypmu, K.ld(op, ypnu, Vh))));                             // T3 = (A U K)^dag
-    macc(acc, t, f);
-    t = mm_nn(mm_na(K.ld(par, ypnummu, Vh), Uymmu), A.ld(op, ymmu, Vh));              // T4
-    macc(acc, t, f);
-    KU.st(par, h, Vh, acc);
+    const M3<R> Ky = narrow<R>(K.ld(par, h, Vh)), Ay = narrow<R>(A.ld(par, h, Vh));
+    M3<R> acc = tnn<R>(tna<R>(narrow<R>(A.ld(op, ypnu, Vh)), Uypmu), Ky);                            // T1
+    tacc<R>(acc, tadj<R>(tnn<R>(narrow<R>(K.ld(op, ymmu, Vh)), tnn<R>(Uymmu, narrow<R>(A.ld(par, ypnummu, Vh))))),
+            (R)1);                                                                                  // T2 = (K U A)^dag
+    tacc<R>(acc, tadj<R>(tnn<R>(Ay, tnn<R>(Uypmu, narrow<R>(K.ld(op, ypnu, Vh))))), (R)1);          // T3 = (A U K)^dag
+    tacc<R>(acc, tnn<R>(tna<R>(narrow<R>(K.ld(par, ypnummu, Vh)), Uymmu), narrow<R>(A.ld(op, ymmu, Vh))),
+            (R)1);                                                                                  // T4
+    M3<double> out = KU.ld(par, h, Vh);
+    macc(out, widen<R>(acc), f);
+    KU.st(par, h, Vh, out);
   }
+  (void)fr;
 }
 
 // reverse of L_mu(x) = c W_mu(x) W_mu(x+mu) W_mu(x+2mu):
@@ -300,7 +305,10 @@ static int staple_fwd(int mu, int nu, MatF Unu, MatF A, MatF S) {
   Context &c = ctx();
   MatF none = {nullptr, 0};
   timing_begin(MKS_K_FORCE);
-  k_staple<<<dim3(grid_for(c.Vh, 128), 2), 128, 0, c.stream>>>(c.geom, mu, nu, Unu, A, none, 0.0, S);
+  if (c.md_prec == MKS_PREC_SINGLE)
+    k_staple<float><<<dim3(grid_for(c.Vh, 128), 2), 128, 0, c.stream>>>(c.geom, mu, nu, Unu, A, none, 0.0, S);
+  else
+    k_staple<double><<<dim3(grid_for(c.Vh, 128), 2), 128, 0, c.stream>>>(c.geom, mu, nu, Unu, A, none, 0.0, S);
   timing_end(MKS_K_FORCE);
   g_force_flops += 4.0 * 198 * c.V;
   MKS_CUDA(cudaGetLastError());
@@ -310,7 +318,10 @@ static int staple_fwd(int mu, int nu, MatF Unu, MatF A, MatF S) {
 static int staple_adj(int mu, int nu, MatF Unu, MatF A, MatF K, double f, MatF KA, MatF KU) {
   Context &c = ctx();
   timing_begin(MKS_K_FORCE);
-  k_staple_adj<<<dim3(grid_for(c.Vh, 128), 2), 128, 0, c.stream>>>(c.geom, mu, nu, Unu, A, K, f, KA, KU);
+  if (c.md_prec == MKS_PREC_SINGLE)
+    k_staple_adj<float><<<dim3(grid_for(c.Vh, 128), 2), 128, 0, c.stream>>>(c.geom, mu, nu, Unu, A, K, f, KA, KU);
+  else
+    k_staple_adj<double><<<dim3(grid_for(c.Vh, 128), 2), 128, 0, c.stream>>>(c.geom, mu, nu, Unu, A, K, f, KA, KU);
   timing_end(MKS_K_FORCE);
   g_force_flops += 12.0 * 198 * c.V;
   MKS_CUDA(cudaGetLastError());

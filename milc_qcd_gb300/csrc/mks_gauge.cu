@@ -917,6 +917,13 @@ int mks_reunitarize(void) {
   return reunitarize_dev();
 }
 
+int mks_md_precision(int prec) {
+  MKS_TRY(check_ready());
+  if (prec != MKS_PREC_DOUBLE && prec != MKS_PREC_SINGLE) return MKS_ERR_ARG;
+  ctx().md_prec = prec;
+  return MKS_OK;
+}
+
 int mks_plaquette(double *ss, double *st) {
   MKS_TRY(check_ready());
   if (!ss || !st) return MKS_ERR_ARG;

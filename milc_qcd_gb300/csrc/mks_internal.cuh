@@ -347,6 +347,11 @@ struct Context {
   double aux_u0 = 1.0;
   // gauge momenta of the molecular dynamics (anti_hermitmat[V][4], device)
   double *mom = nullptr;
+  // arithmetic of the staple products in link construction and the fermion
+  // force (MKS_PREC_DOUBLE, or MKS_PREC_SINGLE inside a molecular-dynamics
+  // integration), and the one the current fermion links were built with
+  int md_prec = MKS_PREC_DOUBLE;
+  int links_prec = MKS_PREC_DOUBLE;
   // timing
   bool timing = false;
   double kernel_ms[MKS_K_COUNT] = {0};

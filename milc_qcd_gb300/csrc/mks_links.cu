@@ -133,7 +133,10 @@ struct FatCoeffs { double one_link, naik, three_staple, five_staple, seven_stapl
 static int launch_staple(int mu, int nu, MatF Unu, MatF A, MatF fat, double coef, MatF sout) {
   Context &c = ctx();
   timing_begin(MKS_K_LINKS);
-  k_staple<<<dim3(grid_for(c.Vh, 128), 2), 128, 0, c.stream>>>(c.geom, mu, nu, Unu, A, fat, coef, sout);
+  if (c.md_prec == MKS_PREC_SINGLE)
+    k_staple<float><<<dim3(grid_for(c.Vh, 128), 2), 128, 0, c.stream>>>(c.geom, mu, nu, Unu, A, fat, coef, sout);
+  else
+    k_staple<double><<<dim3(grid_for(c.Vh, 128), 2), 128, 0, c.stream>>>(c.geom, mu, nu, Unu, A, fat, coef, sout);
   timing_end(MKS_K_LINKS);
   MKS_CUDA(cudaGetLastError());
   return MKS_OK;
@@ -257,6 +260,7 @@ int links_from_aux(int action, int n_naiks, const double *eps_naik, double u0) {
   }
   c.aux_action = action;
   c.aux_u0 = u0;
+  c.links_prec = c.md_prec;
   MKS_CUDA(cudaMemcpyAsync(&g_nsvd, nsvd, sizeof(unsigned int), cudaMemcpyDeviceToHost, c.stream));
   MKS_CUDA(cudaStreamSynchronize(c.stream));
   dev_free(nsvd); dev_free(staple); dev_free(tmp); dev_free(f3); dev_free(l3);

@@ -45,7 +45,7 @@ struct Traj {
 
   int links() {
     Context &c = ctx();
-    if (c.slots[0].valid && c.aux_action == MKS_ACTION_HISQ) return MKS_OK;
+    if (c.slots[0].valid && c.aux_action == MKS_ACTION_HISQ && c.links_prec == c.md_prec) return MKS_OK;
     const double t0 = wall();
     MKS_TRY(links_from_aux(MKS_ACTION_HISQ, (int)eps_distinct.size(), eps_distinct.data(), 1.0));
     r->t_links += wall() - t0;
@@ -132,8 +132,7 @@ struct Traj {
 
   int update_h_gauge(double eps) {
     const double t0 = wall();
-    MKS_TRY(gauge_force_dev(eps, p->beta, p->u0, p->nflavors,
-                            p->prec_gauge_force == MKS_PREC_SINGLE ? MKS_PREC_SINGLE : MKS_PREC_DOUBLE));
+    MKS_TRY(gauge_force_dev(eps, p->beta, p->u0, p->nflavors, ctx().md_prec));
     MKS_CUDA(cudaStreamSynchronize(ctx().stream));
     r->t_gauge_force += wall() - t0;
     r->n_gauge_force++;
@@ -257,7 +256,12 @@ struct Traj {
       MKS_TRY(grsource());
     }
     MKS_TRY(action(&r->g0, &r->h0, &r->f0));
-    MKS_TRY(integrate());
+    // forces and the links rebuilt for them in the arithmetic asked for;
+    // the action before and after is always evaluated in FP64
+    c.md_prec = p->prec_force == MKS_PREC_SINGLE ? MKS_PREC_SINGLE : MKS_PREC_DOUBLE;
+    int rc = integrate();
+    c.md_prec = MKS_PREC_DOUBLE;
+    MKS_TRY(rc);
     MKS_TRY(action(&r->g1, &r->h1, &r->f1));
     r->delta_s = (r->g1 + r->h1 + r->f1) - (r->g0 + r->h0 + r->f0);
     MKS_TRY(plaquette_dev(&r->plaq_ss, &r->plaq_st));

@@ -75,6 +75,94 @@ __device__ __forceinline__ M3<double> mm_an(const M3<double> &a, const M3<double
   return c;
 }
 
+// the same products in arithmetic R (FP64 fields converted on load and back
+// on store: FP32 arithmetic runs at many times the FP64 rate on GB300)
+template <typename R>
+__device__ __forceinline__ M3<R> narrow(const M3<double> &m) {
+  M3<R> o;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) o.e[i][j] = {(R)m.e[i][j].re, (R)m.e[i][j].im};
+  return o;
+}
+template <typename R>
+__device__ __forceinline__ M3<double> widen(const M3<R> &m) {
+  M3<double> o;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) o.e[i][j] = {(double)m.e[i][j].re, (double)m.e[i][j].im};
+  return o;
+}
+template <typename R>
+__device__ __forceinline__ M3<R> tnn(const M3<R> &a, const M3<R> &b) {
+  M3<R> c;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      R re = 0, im = 0;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        re = fma(a.e[i][k].re, b.e[k][j].re, re); re = fma(-a.e[i][k].im, b.e[k][j].im, re);
+        im = fma(a.e[i][k].re, b.e[k][j].im, im); im = fma(a.e[i][k].im, b.e[k][j].re, im);
+      }
+      c.e[i][j] = {re, im};
+    }
+  return c;
+}
+template <typename R>
+__device__ __forceinline__ M3<R> tna(const M3<R> &a, const M3<R> &b) {  // a b^dag
+  M3<R> c;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      R re = 0, im = 0;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        re = fma(a.e[i][k].re, b.e[j][k].re, re); re = fma(a.e[i][k].im, b.e[j][k].im, re);
+        im = fma(a.e[i][k].im, b.e[j][k].re, im); im = fma(-a.e[i][k].re, b.e[j][k].im, im);
+      }
+      c.e[i][j] = {re, im};
+    }
+  return c;
+}
+template <typename R>
+__device__ __forceinline__ M3<R> tan_(const M3<R> &a, const M3<R> &b) {  // a^dag b
+  M3<R> c;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      R re = 0, im = 0;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        re = fma(a.e[k][i].re, b.e[k][j].re, re); re = fma(a.e[k][i].im, b.e[k][j].im, re);
+        im = fma(a.e[k][i].re, b.e[k][j].im, im); im = fma(-a.e[k][i].im, b.e[k][j].re, im);
+      }
+      c.e[i][j] = {re, im};
+    }
+  return c;
+}
+template <typename R>
+__device__ __forceinline__ M3<R> tadj(const M3<R> &a) {
+  M3<R> c;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) c.e[i][j] = {a.e[j][i].re, -a.e[j][i].im};
+  return c;
+}
+template <typename R>
+__device__ __forceinline__ void tacc(M3<R> &d, const M3<R> &s, R f) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) { d.e[i][j].re = fma(f, s.e[i][j].re, d.e[i][j].re); d.e[i][j].im = fma(f, s.e[i][j].im, d.e[i][j].im); }
+}
+
 // neighbour (checkerboard index) of site (par,h) displaced by d along mu
 __device__ __forceinline__ int nbr(const Geom &g, int par, int h, int mu, int d) {
   int c[4];
@@ -94,9 +182,11 @@ __device__ __forceinline__ int nbr2(const Geom &g, int par, int h, int mu, int d
 
 // generalised staple S(x) = U_nu(x) A(x+nu) U_nu(x+mu)^dag + U_nu(x-nu)^dag A(x-nu) U_nu(x-nu+mu)
 // (generic/general_staple.c:42-140): S saved when sout.p != nullptr, and
-// fat_mu(x) += coef * S(x) when fat.p != nullptr
+// fat_mu(x) += coef * S(x) when fat.p != nullptr; products in arithmetic R,
+// fields and the accumulation FP64
+template <typename R>
 static __global__ void __launch_bounds__(128) k_staple(Geom g, int mu, int nu, MatF Unu, MatF A, MatF fat, double coef,
-                                                MatF sout) {
+                                                       MatF sout) {
   const int h = blockIdx.x * blockDim.x + threadIdx.x;
   const int par = blockIdx.y, opar = 1 - par;
   const int Vh = g.Vh;
@@ -104,14 +194,17 @@ static __global__ void __launch_bounds__(128) k_staple(Geom g, int mu, int nu, M
   const int xpnu = nbr(g, par, h, nu, 1), xpmu = nbr(g, par, h, mu, 1), xmnu = nbr(g, par, h, nu, -1);
   const int xmnupmu = nbr2(g, par, h, nu, -1, mu, 1);
   // upper: U_nu(x) [A(x+nu) U_nu(x+mu)^dag]
-  M3<double> up = mm_nn(Unu.ld(par, h, Vh), mm_na(A.ld(opar, xpnu, Vh), Unu.ld(opar, xpmu, Vh)));
+  M3<R> up = tnn<R>(narrow<R>(Unu.ld(par, h, Vh)),
+                    tna<R>(narrow<R>(A.ld(opar, xpnu, Vh)), narrow<R>(Unu.ld(opar, xpmu, Vh))));
   // lower: [U_nu(x-nu)^dag A(x-nu)] U_nu(x-nu+mu)
-  M3<double> dn = mm_nn(mm_an(Unu.ld(opar, xmnu, Vh), A.ld(opar, xmnu, Vh)), Unu.ld(par, xmnupmu, Vh));
+  M3<R> dn = tnn<R>(tan_<R>(narrow<R>(Unu.ld(opar, xmnu, Vh)), narrow<R>(A.ld(opar, xmnu, Vh))),
+                    narrow<R>(Unu.ld(par, xmnupmu, Vh)));
   M3<double> s;
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
-    for (int j = 0; j < 3; j++) s.e[i][j] = {up.e[i][j].re + dn.e[i][j].re, up.e[i][j].im + dn.e[i][j].im};
+    for (int j = 0; j < 3; j++)
+      s.e[i][j] = {(double)up.e[i][j].re + (double)dn.e[i][j].re, (double)up.e[i][j].im + (double)dn.e[i][j].im};
   if (sout.p) sout.st(par, h, Vh, s);
   if (!fat.p) return;
   M3<double> f = fat.ld(par, h, Vh);

@@ -96,7 +96,7 @@ INTEGRATORS = {"leapfrog": 0, "omelyan": 1, "2G1F": 2, "3G1F": 3}
 
 def update(pseudofermions, beta, u0, nflavors, epsilon, steps, int_alg="3G1F", resid_md=None, resid_fa=None,
            resid_gr=None, max_cg=2500, prec_md=2, prec_fa=2, prec_gr=2, nrestart=5, refresh=True,
-           prec_gauge_force=2):
+           prec_force=2):
     """MILC's update() (ks_imp_rhmc/update_rhmc.c) on the resident links and
     momenta.  pseudofermions: list of PseudofermionParams (or dicts with
     'MD'/'GR'/'FA' -> (res, pole) and 'naik_term_epsilon'); resid_*: one
@@ -129,7 +129,7 @@ def update(pseudofermions, beta, u0, nflavors, epsilon, steps, int_alg="3G1F", r
                                     resid_gr[i], int(max_cg))
     p = _lib.RhmcParams(beta, u0, int(nflavors), epsilon, int(steps), INTEGRATORS[int_alg], n,
                         ctypes.cast(arr, ctypes.POINTER(_lib.Pseudofermion)), prec_md, prec_fa, prec_gr,
-                        int(nrestart), 1 if refresh else 0, int(prec_gauge_force))
+                        int(nrestart), 1 if refresh else 0, int(prec_force))
     r = _lib.RhmcResult()
     check(init().mks_rhmc_trajectory(ctypes.byref(p), ctypes.byref(r)), "mks_rhmc_trajectory")
     out = {f: getattr(r, f) for f, _ in _lib.RhmcResult._fields_ if f != "grsource_sum"}

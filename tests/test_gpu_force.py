@@ -5,7 +5,7 @@ Spec tolerance: 1e-10 relative."""
 import numpy as np
 import pytest
 
-from conftest import rel
+from conftest import hisq_setup, rel
 
 pytestmark = pytest.mark.gpu
 
@@ -49,3 +49,23 @@ def test_force_is_linear_in_eps_and_accumulates(gpu, oracle_cls):
     m.eo_fermion_force_multi(0.05, [1.0], xxx, b)
     m.eo_fermion_force_multi(0.05, [1.0], xxx, b)
     assert rel(b[..., :9], a[..., :9]) < 1e-13
+
+
+def test_force_fp32_arithmetic(gpu, oracle_cls):
+    """FP32 staple products (molecular-dynamics setting) against the FP64
+    oracle force: relative 1e-5."""
+    m = gpu
+    dims = (4, 4, 4, 8)
+    U, orc, L = hisq_setup(m, oracle_cls, dims, eps_naik=(0.0, -0.1))
+    m.set_lattice(dims)
+    xxx = [m.gen_vector(dims, 91 + j, m.EVENANDODD) for j in range(3)]
+    res, orders = [0.2, 0.5, 0.9], [2, 1]
+    want = orc.fermion_force_hisq(U, 0.07, res, np.stack(xxx), orders=orders, eps_naik=(0.0, -0.1))
+    try:
+        m.md_precision(m.PREC_SINGLE)
+        m.load_hisq_links(U, (0.0, -0.1))
+        mom = np.zeros_like(want)
+        m.eo_fermion_force_multi(0.07, res, xxx, mom, n_orders_naik=orders, n_naiks=2)
+    finally:
+        m.md_precision(m.PREC_DOUBLE)
+    assert rel(mom, want) < 1e-5

@@ -22,7 +22,7 @@ def _run(m, prec):
     m.rng_seed(R.ISEED)
     pfs = [dict(d["rational"][i], naik_term_epsilon=float(d["naik_eps"][i])) for i in range(R.N_PSEUDO)]
     return update(pfs, R.BETA, R.U0, R.nflavors(), R.EPSILON, R.STEPS, R.INT_ALG, R.RESID_MD, R.RESID_FA,
-                  R.RESID_GR, R.MAX_CG, prec, prec, prec, R.NRESTART, True)
+                  R.RESID_GR, R.MAX_CG, prec, prec, prec, R.NRESTART, True, prec_force=prec)
 
 
 def test_trajectory_fp64_reproduces_milc_sample(gpu):
