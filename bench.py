@@ -438,6 +438,53 @@ def gpu_arm(args):
     print(json.dumps(line), flush=True)
 
 
+# 2+1+1 HISQ RHMC trajectory (the molecular-dynamics workload): 48^3x96,
+# masses 0.0012 / 0.0363 / 0.432 (rational functions generated by
+# milc_qcd_gb300/data/make_rationals.py), links from seeded exp(i 0.2 H),
+# 10 leapfrog steps, tau = 1; once with FP32 solves and force arithmetic
+# and once all FP64 from the same start (Delta H against the FP64 run).
+RHMC_WORKLOAD = dict(dims=(48, 48, 48, 96), beta=6.3, u0=0.86, nflavors=4, steps=10, tau=1.0,
+                     rationals="rationals.hisq_2p1p1_ml0.0012_ms0.0363_mc0.432.txt",
+                     resid_md=1e-6, resid_fa=1e-10, resid_gr=1e-10, max_cg=5000, seed=7)
+
+
+def rhmc_workload(args):
+    import milc_qcd_gb300 as m
+    from milc_qcd_gb300.rhmc import load_rhmc_params, update
+    w = dict(RHMC_WORKLOAD)
+    if args.dims:
+        w["dims"] = tuple(args.dims)
+    dims = w["dims"]
+    pfs = load_rhmc_params(os.path.join(ROOT, "milc_qcd_gb300", "data", w["rationals"]))
+    n = len(pfs)
+    m.init(0)
+    m.set_lattice(dims)
+    V = int(np.prod(dims))
+    U0 = m.gen_thin_links(dims, w["seed"], 0.2)
+    runs = {}
+    with Clocks() as clk:
+        for name, prec in (("f32", m.PREC_SINGLE), ("f64", m.PREC_DOUBLE)):
+            m.gauge_load(U0)
+            m.mom_load(np.zeros((V, 4, 10)))
+            m.rng_seed(w["seed"])
+            r = update(pfs, w["beta"], w["u0"], w["nflavors"], w["tau"] / w["steps"], w["steps"], "leapfrog",
+                       [w["resid_md"]] * n, [w["resid_fa"]] * n, [w["resid_gr"]] * n, w["max_cg"], prec, prec, prec,
+                       5, True, prec_force=prec)
+            runs[name] = {k: r[k] for k in ("t_total", "t_solve", "t_fermion_force", "t_gauge_force", "t_links",
+                                             "cg_iters", "n_solves", "unconverged", "delta_s", "start", "end")}
+    line = {"metric": "RHMC s per trajectory (2+1+1 HISQ, %s)" % "x".join(map(str, dims)),
+            "value": runs["f32"]["t_total"], "unit": "s/trajectory", "n_gpus": 1, "steps": 1, "warmup": 0,
+            "higher_is_better": False, "dtype": "f32+f64", "data": "synthetic (seeded exp(i 0.2 H) links)",
+            "config": {"workload": "2+1+1 HISQ RHMC trajectory, leapfrog 10 steps, tau 1", "lattice": list(dims),
+                       "masses": [0.0012, 0.0363, 0.432], "beta": w["beta"], "u0": w["u0"],
+                       "pseudofermions": n, "poles": [p.MD.order for p in pfs],
+                       "resid_md_fa_gr": [w["resid_md"], w["resid_fa"], w["resid_gr"]]},
+            "delta_h_f32": runs["f32"]["delta_s"], "delta_h_f64": runs["f64"]["delta_s"],
+            "delta_h_f32_minus_f64": runs["f32"]["delta_s"] - runs["f64"]["delta_s"],
+            "runs": runs, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -453,7 +500,15 @@ def main():
     ap.add_argument("--ref-iters", type=int, default=int(os.environ.get("MKS_REF_ITERS", "0")) or None)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--workload", default="cg", choices=["cg", "rhmc"],
+                    help="cg: the headline CG benchmark; rhmc: one 2+1+1 HISQ RHMC trajectory")
     args = ap.parse_args()
+    if args.workload == "rhmc":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the rhmc workload has no CPU reference arm"}))
+            return
+        rhmc_workload(args)
+        return
     if args.dims:
         global DIMS
         DIMS = tuple(args.dims)
