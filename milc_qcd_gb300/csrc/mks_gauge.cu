@@ -56,6 +56,36 @@ __device__ __forceinline__ M3<double> load_link(const Geom &g, const double2 *U,
   return m;
 }
 
+// unphased FP32 copy of the thin links, same [2][4][9][Vh] layout: the FP32
+// gauge force walks ~230 links per output link through L1/L2, so halving
+// the bytes of every link fetched matters more than the conversion pass
+__global__ void __launch_bounds__(128) k_thin_to_f32(Geom g, const double2 *U, float2 *U32) {
+  const int h = blockIdx.x * blockDim.x + threadIdx.x, par = blockIdx.y, mu = blockIdx.z;
+  if (h >= g.Vh) return;
+  int c[4];
+  site_coords(g, par, h, c[0], c[1], c[2], c[3]);
+  const float ph = (float)stag_phase(g, c, mu);
+  const size_t base = ((size_t)par * 4 + mu) * 9 * g.Vh + h;
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    const double2 a = U[base + (size_t)k * g.Vh];
+    U32[base + (size_t)k * g.Vh] = make_float2(ph * (float)a.x, ph * (float)a.y);
+  }
+}
+
+__device__ __forceinline__ M3<float> load_link32(const Geom &g, const float2 *U32, const int c[4], int dir) {
+  const int par = (c[0] + c[1] + c[2] + c[3]) & 1;
+  const int h = cb_index(g, c[0], c[1], c[2], c[3]);
+  const float2 *b = U32 + ((size_t)par * 4 + dir) * 9 * g.Vh + h;
+  M3<float> m;
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    const float2 a = __ldg(b + (size_t)k * g.Vh);
+    m.e[k / 3][k % 3] = {a.x, a.y};
+  }
+  return m;
+}
+
 // ------------------------------------------------------------------ paths
 constexpr int GPATH_MAX = 64;
 struct LoopPaths {       // every loop orientation of the action (34 for Symanzik 1-loop)
@@ -277,13 +307,37 @@ __device__ __forceinline__ M3<double> walk(const Geom &g, const double2 *U, int 
   return walk_r<double>(g, U, c, path, len);
 }
 
+// the same walk on the unphased FP32 copy
+__device__ __forceinline__ M3<float> walk32(const Geom &g, const float2 *U32, int c[4], const signed char *path,
+                                            int len) {
+  const int L[4] = {g.nx, g.ny, g.nz, g.nt};
+  M3<float> P;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) P.e[i][j] = {i == j ? 1.f : 0.f, 0.f};
+  for (int k = 0; k < len; k++) {
+    const int d = path[k];
+    if (d < 4) {
+      P = mul_nn<float>(P, load_link32(g, U32, c, d));
+      c[d] = wrap_add(c[d], 1, L[d]);
+    } else {
+      const int dd = 7 - d;
+      c[dd] = wrap_add(c[dd], -1, L[dd]);
+      P = mul_na<float>(P, load_link32(g, U32, c, dd));
+    }
+  }
+  return P;
+}
+
 // mom_mu(x) <- TA(mom_mu(x) - eb3 U_mu(x) sum_p c_p Q_p), Q_p the staple
 // paths from x+mu back to x (links without phases)
 // staple sum and product in arithmetic R (FP64 reproduces MILC's double
 // build; FP32 runs at the FP32 rate for large-lattice molecular dynamics);
 // the momentum update is FP64 either way
 template <typename R>
-__global__ void __launch_bounds__(128) k_gauge_force(Geom g, const double2 *U, double *mom, double eb3) {
+__global__ void __launch_bounds__(128) k_gauge_force(Geom g, const double2 *U, const float2 *U32, double *mom,
+                                                     double eb3) {
   const int h = blockIdx.x * blockDim.x + threadIdx.x, par = blockIdx.y, mu = blockIdx.z;
   if (h >= g.Vh) return;
   int x0[4];
@@ -298,7 +352,9 @@ __global__ void __launch_bounds__(128) k_gauge_force(Geom g, const double2 *U, d
   for (int p = 0; p < np; p++) {
     int c[4] = {x0[0], x0[1], x0[2], x0[3]};
     c[mu] = wrap_add(c[mu], 1, L[mu]);
-    const M3<R> Q = walk_r<R>(g, U, c, c_staples.dir[mu][p], c_staples.len[mu][p]);
+    M3<R> Q;
+    if constexpr (sizeof(R) == 4) Q = walk32(g, U32, c, c_staples.dir[mu][p], c_staples.len[mu][p]);
+    else Q = walk_r<R>(g, U, c, c_staples.dir[mu][p], c_staples.len[mu][p]);
     const R cf = (R)c_staples.c[mu][p];
 #pragma unroll
     for (int i = 0; i < 3; i++)
@@ -308,7 +364,10 @@ __global__ void __launch_bounds__(128) k_gauge_force(Geom g, const double2 *U, d
         S.e[i][j].im = fma(cf, Q.e[i][j].im, S.e[i][j].im);
       }
   }
-  const M3<R> Gr = mul_nn<R>(to_r<R>(load_link(g, U, x0, mu, true)), S);
+  M3<R> Ux;
+  if constexpr (sizeof(R) == 4) Ux = load_link32(g, U32, x0, mu);
+  else Ux = to_r<R>(load_link(g, U, x0, mu, true));
+  const M3<R> Gr = mul_nn<R>(Ux, S);
   M3<double> G;
 #pragma unroll
   for (int i = 0; i < 3; i++)
@@ -629,6 +688,8 @@ __global__ void k_lincomb(Geom g, int par, LinComb lc, double *out) {
 // ------------------------------------------------------------------ host side
 static SitePrn *g_prn = nullptr;
 static size_t g_prn_sites = 0;
+static float2 *g_u32 = nullptr;  // unphased FP32 thin links for the FP32 gauge force
+static size_t g_u32_sites = 0;
 
 static int ensure_mom() {
   Context &c = ctx();
@@ -663,10 +724,19 @@ int gauge_force_dev(double eps, double beta, double u0, int nflavors, int prec) 
   Context &c = ctx();
   MKS_TRY(upload_paths(nflavors, u0));
   timing_begin(MKS_K_GAUGE);
-  if (prec == MKS_PREC_DOUBLE)
-    k_gauge_force<double><<<link_grid(), 128, 0, c.stream>>>(c.geom, c.auxU, c.mom, eps * beta / 3.0);
-  else
-    k_gauge_force<float><<<link_grid(), 128, 0, c.stream>>>(c.geom, c.auxU, c.mom, eps * beta / 3.0);
+  if (prec == MKS_PREC_DOUBLE) {
+    k_gauge_force<double><<<link_grid(), 128, 0, c.stream>>>(c.geom, c.auxU, nullptr, c.mom, eps * beta / 3.0);
+  } else {
+    if (g_u32_sites != c.V) {
+      dev_free(g_u32);
+      g_u32 = nullptr;
+      g_u32_sites = 0;
+      MKS_TRY(dev_alloc((void **)&g_u32, c.V * 36 * sizeof(float2)));
+      g_u32_sites = c.V;
+    }
+    k_thin_to_f32<<<link_grid(), 128, 0, c.stream>>>(c.geom, c.auxU, g_u32);
+    k_gauge_force<float><<<link_grid(), 128, 0, c.stream>>>(c.geom, c.auxU, g_u32, c.mom, eps * beta / 3.0);
+  }
   timing_end(MKS_K_GAUGE);
   MKS_CUDA(cudaGetLastError());
   return MKS_OK;
@@ -782,6 +852,9 @@ void gauge_free() {
   dev_free(g_prn);
   g_prn = nullptr;
   g_prn_sites = 0;
+  dev_free(g_u32);
+  g_u32 = nullptr;
+  g_u32_sites = 0;
 }
 
 static int host_io(double *host, double *dev, size_t bytes, bool up) {
