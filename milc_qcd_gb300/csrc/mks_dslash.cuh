@@ -62,8 +62,14 @@ struct NoFinish {
   __device__ void operator()(const double *, int) const {}
 };
 
+// minimum resident 256-thread blocks per SM asked of the register allocator
+// for the kernels with up to 4 sources per thread (0: no request)
+#ifndef MKS_DSLASH_MINB
+#define MKS_DSLASH_MINB 0
+#endif
+
 template <typename R, class LinkT, class InT, class OutT, int NB, int EPI, int NSUM, class Fin>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, (MKS_DSLASH_MINB > 0 && NB <= 4) ? MKS_DSLASH_MINB : 1)
 k_dslash(const LinkT fat, const LinkT lng, const DslashArgs<InT, OutT, typename EpiLoad<R>::type> a,
          const Fin fin) {
   typedef typename EpiLoad<R>::type EpiT;

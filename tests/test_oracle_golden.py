@@ -81,7 +81,7 @@ def test_oracle_force_matches_milc(oracle_cls, hisq):
                                  orders=list(hisq["ff_orders"]), eps_naik=tuple(hisq["eps_naik"]),
                                  mom=hisq["ff_mom0"])
     d, dr = mom - hisq["ff_mom0"], hisq["ff_mom"] - hisq["ff_mom0"]
-    assert rel(d[..., :9], dr[..., :9]) < 1e-12  # spec: 1e-10
+    assert rel(d[..., :9], dr[..., :9]) < 1e-12  # forces are required to agree within 1e-10
 
 
 def test_oracle_asqtad(oracle_cls, asqtad):
