@@ -346,11 +346,13 @@ int mks_update_u(double eps);
 int mks_mom_action(double *h);
 int mks_reunitarize(void);
 int mks_plaquette(double *ss, double *st);
-/* Arithmetic of the staple products in later link constructions
- * (mks_load_links_from_thin, mks_rebuild_links) and fermion forces:
- * MKS_PREC_DOUBLE (the default, MILC's double build) or MKS_PREC_SINGLE
- * (FP32 products, FP64 fields and accumulation; for molecular-dynamics
- * forces).  No reference counterpart: MILC's CPU force is FP64. */
+/* Precision of later link constructions (mks_load_links_from_thin,
+ * mks_rebuild_links) and fermion forces: MKS_PREC_DOUBLE (the default,
+ * MILC's double build) or MKS_PREC_SINGLE (for molecular-dynamics forces:
+ * the smearing stages, staples and force adjoints stored and multiplied in
+ * FP32; the U(3) projection and its adjoint in FP64 arithmetic; the
+ * resident links, the slots' fat / long links and the momentum update stay
+ * FP64 fields).  No reference counterpart: MILC's CPU force is FP64. */
 int mks_md_precision(int prec);
 
 /* ------------------------------------------------------------------ */

@@ -67,9 +67,14 @@ struct NoFinish {
 #ifndef MKS_DSLASH_MINB
 #define MKS_DSLASH_MINB 0
 #endif
+#if MKS_DSLASH_MINB > 0
+#define MKS_DSLASH_BOUNDS(NB) __launch_bounds__(256, (NB) <= 4 ? MKS_DSLASH_MINB : 1)
+#else
+#define MKS_DSLASH_BOUNDS(NB) __launch_bounds__(256)
+#endif
 
 template <typename R, class LinkT, class InT, class OutT, int NB, int EPI, int NSUM, class Fin>
-__global__ void __launch_bounds__(256, (MKS_DSLASH_MINB > 0 && NB <= 4) ? MKS_DSLASH_MINB : 1)
+__global__ void MKS_DSLASH_BOUNDS(NB)
 k_dslash(const LinkT fat, const LinkT lng, const DslashArgs<InT, OutT, typename EpiLoad<R>::type> a,
          const Fin fin) {
   typedef typename EpiLoad<R>::type EpiT;

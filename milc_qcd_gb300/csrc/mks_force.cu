@@ -29,44 +29,60 @@
 
 namespace mks {
 
-__device__ __forceinline__ M3<double> adjm(const M3<double> &a) {
-  M3<double> c;
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) c.e[i][j] = {a.e[j][i].re, -a.e[j][i].im};
-  return c;
-}
-__device__ __forceinline__ void macc(M3<double> &d, const M3<double> &s, double f) {
+// d += f s in precision R
+template <typename R>
+__device__ __forceinline__ void macc(M3<R> &d, const M3<R> &s, R f) {
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = 0; j < 3; j++) { d.e[i][j].re += f * s.e[i][j].re; d.e[i][j].im += f * s.e[i][j].im; }
 }
+template <typename R>
+__device__ __forceinline__ M3<double> to64(const M3<R> &a) {
+  M3<double> c;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) c.e[i][j] = {(double)a.e[i][j].re, (double)a.e[i][j].im};
+  return c;
+}
+template <typename R>
+__device__ __forceinline__ M3<R> from64(const M3<double> &a) {
+  M3<R> c;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) c.e[i][j] = {(R)a.e[i][j].re, (R)a.e[i][j].im};
+  return c;
+}
 
 // 1. level-0 outer products for terms [j0, j1), scaled by `scale`
+template <typename R>
 struct OuterArgs {
-  const double2 *x[64];   // full-lattice SoA [2][3][Vh] per term
+  const typename Stor<R>::t *x[64];   // full-lattice SoA [2][3][Vh] per term
   double res[64];
   int j0, j1;
   double scale;
 };
-__global__ void __launch_bounds__(128) k_outer(Geom g, OuterArgs a, double2 *Kf, double2 *Kl) {
+template <typename R>
+__global__ void __launch_bounds__(128) k_outer(Geom g, OuterArgs<R> a, typename Stor<R>::t *Kf,
+                                               typename Stor<R>::t *Kl) {
+  typedef typename Stor<R>::t T2;
   const int h = blockIdx.x * blockDim.x + threadIdx.x;
   const int par = blockIdx.y, mu = blockIdx.z;
   const int Vh = g.Vh;
   if (h >= Vh) return;
   const int y1 = nbr(g, par, h, mu, 1), y3 = nbr(g, par, h, mu, 3);
   const double s = par == 0 ? a.scale : -a.scale;
-  MatF F = link_dir(Kf, mu, Vh), L = link_dir(Kl, mu, Vh);
-  M3<double> kf = F.ld(par, h, Vh), kl = L.ld(par, h, Vh);
+  MatT<R> F = link_dir(Kf, mu, Vh), L = link_dir(Kl, mu, Vh);
+  M3<R> kf = F.ld(par, h, Vh), kl = L.ld(par, h, Vh);
   for (int j = a.j0; j < a.j1; j++) {
-    const double2 *x = a.x[j];
-    const double r = s * a.res[j];
-    cplx<double> b[3], u1[3], u3[3];
+    const T2 *x = a.x[j];
+    const R r = (R)(s * a.res[j]);
+    cplx<R> b[3], u1[3], u3[3];
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-      double2 q = x[((size_t)par * 3 + c) * Vh + h];
+      T2 q = x[((size_t)par * 3 + c) * Vh + h];
       b[c] = {q.x, q.y};
       q = x[((size_t)(1 - par) * 3 + c) * Vh + y1];
       u1[c] = {q.x, q.y};
@@ -93,9 +109,10 @@ __global__ void __launch_bounds__(128) k_outer(Geom g, OuterArgs a, double2 *Kf,
 //   KA(y)    += U_nu(y-nu+mu)^dag K(y-nu) U_nu(y-nu) + U_nu(y+mu) K(y+nu) U_nu(y)^dag
 //   KUnu(y)  += A(y+nu) U_nu(y+mu)^dag K(y) + A(y-mu+nu)^dag U_nu(y-mu)^dag K(y-mu)^dag
 //             + K(y+nu)^dag U_nu(y+mu)^dag A(y)^dag + K(y+nu-mu) U_nu(y-mu)^dag A(y-mu)
+// Fields stored and products computed in precision R.
 template <typename R>
-__global__ void __launch_bounds__(128) k_staple_adj(Geom g, int mu, int nu, MatF Unu, MatF A, MatF K, double f,
-                                                    MatF KA, MatF KU) {
+__global__ void __launch_bounds__(128) k_staple_adj(Geom g, int mu, int nu, MatT<R> Unu, MatT<R> A, MatT<R> K,
+                                                    double f, MatT<R> KA, MatT<R> KU) {
   const int h = blockIdx.x * blockDim.x + threadIdx.x;
   const int par = blockIdx.y, op = 1 - par;
   const int Vh = g.Vh;
@@ -103,54 +120,55 @@ __global__ void __launch_bounds__(128) k_staple_adj(Geom g, int mu, int nu, MatF
   const int ymnu = nbr(g, par, h, nu, -1), ypnu = nbr(g, par, h, nu, 1), ypmu = nbr(g, par, h, mu, 1);
   const int ymmu = nbr(g, par, h, mu, -1);
   const int ymnupmu = nbr2(g, par, h, nu, -1, mu, 1), ypnummu = nbr2(g, par, h, nu, 1, mu, -1);
-  const M3<R> Uy = narrow<R>(Unu.ld(par, h, Vh));
-  const M3<R> Uypmu = narrow<R>(Unu.ld(op, ypmu, Vh));
-  const M3<R> Uymmu = narrow<R>(Unu.ld(op, ymmu, Vh));
+  const M3<R> Uy = Unu.ld(par, h, Vh);
+  const M3<R> Uypmu = Unu.ld(op, ypmu, Vh);
+  const M3<R> Uymmu = Unu.ld(op, ymmu, Vh);
   const R fr = (R)f;
   // KA
   {
-    const M3<R> Uymnu = narrow<R>(Unu.ld(op, ymnu, Vh));
-    const M3<R> Uymnupmu = narrow<R>(Unu.ld(par, ymnupmu, Vh));
-    M3<R> acc = tnn<R>(tan_<R>(Uymnupmu, narrow<R>(K.ld(op, ymnu, Vh))), Uymnu);
-    const M3<R> t = tna<R>(tnn<R>(Uypmu, narrow<R>(K.ld(op, ypnu, Vh))), Uy);
+    const M3<R> Uymnu = Unu.ld(op, ymnu, Vh);
+    const M3<R> Uymnupmu = Unu.ld(par, ymnupmu, Vh);
+    M3<R> acc = tnn<R>(tan_<R>(Uymnupmu, K.ld(op, ymnu, Vh)), Uymnu);
+    const M3<R> t = tna<R>(tnn<R>(Uypmu, K.ld(op, ypnu, Vh)), Uy);
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
       for (int j = 0; j < 3; j++) { acc.e[i][j].re += t.e[i][j].re; acc.e[i][j].im += t.e[i][j].im; }
-    M3<double> out = KA.ld(par, h, Vh);
-    macc(out, widen<R>(acc), f);
+    M3<R> out = KA.ld(par, h, Vh);
+    macc<R>(out, acc, fr);
     KA.st(par, h, Vh, out);
   }
   // KU_nu
   {
-    const M3<R> Ky = narrow<R>(K.ld(par, h, Vh)), Ay = narrow<R>(A.ld(par, h, Vh));
-    M3<R> acc = tnn<R>(tna<R>(narrow<R>(A.ld(op, ypnu, Vh)), Uypmu), Ky);                            // T1
-    tacc<R>(acc, tadj<R>(tnn<R>(narrow<R>(K.ld(op, ymmu, Vh)), tnn<R>(Uymmu, narrow<R>(A.ld(par, ypnummu, Vh))))),
-            (R)1);                                                                                  // T2 = (K U A)^dag
-    tacc<R>(acc, tadj<R>(tnn<R>(Ay, tnn<R>(Uypmu, narrow<R>(K.ld(op, ypnu, Vh))))), (R)1);          // T3 = (A U K)^dag
-    tacc<R>(acc, tnn<R>(tna<R>(narrow<R>(K.ld(par, ypnummu, Vh)), Uymmu), narrow<R>(A.ld(op, ymmu, Vh))),
-            (R)1);                                                                                  // T4
-    M3<double> out = KU.ld(par, h, Vh);
-    macc(out, widen<R>(acc), f);
+    const M3<R> Ky = K.ld(par, h, Vh), Ay = A.ld(par, h, Vh);
+    M3<R> acc = tnn<R>(tna<R>(A.ld(op, ypnu, Vh), Uypmu), Ky);                                       // T1
+    tacc<R>(acc, tadj<R>(tnn<R>(K.ld(op, ymmu, Vh), tnn<R>(Uymmu, A.ld(par, ypnummu, Vh)))), (R)1);  // T2 = (K U A)^dag
+    tacc<R>(acc, tadj<R>(tnn<R>(Ay, tnn<R>(Uypmu, K.ld(op, ypnu, Vh)))), (R)1);                      // T3 = (A U K)^dag
+    tacc<R>(acc, tnn<R>(tna<R>(K.ld(par, ypnummu, Vh), Uymmu), A.ld(op, ymmu, Vh)), (R)1);           // T4
+    M3<R> out = KU.ld(par, h, Vh);
+    macc<R>(out, acc, fr);
     KU.st(par, h, Vh, out);
   }
-  (void)fr;
 }
 
 // reverse of L_mu(x) = c W_mu(x) W_mu(x+mu) W_mu(x+2mu):
 //   KW(y) += c [W(y+mu) W(y+2mu) K(y) + W(y+mu) K(y-mu) W(y-mu) + K(y-2mu) W(y-2mu) W(y-mu)]
-__global__ void __launch_bounds__(128) k_naik_adj(Geom g, const double2 *W, const double2 *Kl, double2 *KW, double c) {
+template <typename R>
+__global__ void __launch_bounds__(128) k_naik_adj(Geom g, const typename Stor<R>::t *W, const typename Stor<R>::t *Kl,
+                                                  typename Stor<R>::t *KW, double c) {
+  typedef typename Stor<R>::t T2;
   const int h = blockIdx.x * blockDim.x + threadIdx.x;
   const int par = blockIdx.y, mu = blockIdx.z, op = 1 - par;
   const int Vh = g.Vh;
   if (h >= Vh) return;
-  MatF Wm = link_dir((double2 *)W, mu, Vh), Km = link_dir((double2 *)Kl, mu, Vh), Om = link_dir(KW, mu, Vh);
+  MatT<R> Wm = link_dir((T2 *)W, mu, Vh), Km = link_dir((T2 *)Kl, mu, Vh), Om = link_dir(KW, mu, Vh);
   const int p1 = nbr(g, par, h, mu, 1), p2 = nbr(g, par, h, mu, 2), m1 = nbr(g, par, h, mu, -1), m2 = nbr(g, par, h, mu, -2);
-  const M3<double> Wp1 = Wm.ld(op, p1, Vh), Wm1 = Wm.ld(op, m1, Vh);
-  M3<double> acc = Om.ld(par, h, Vh);
-  macc(acc, mm_nn(mm_nn(Wp1, Wm.ld(par, p2, Vh)), Km.ld(par, h, Vh)), c);
-  macc(acc, mm_nn(mm_nn(Wp1, Km.ld(op, m1, Vh)), Wm1), c);
-  macc(acc, mm_nn(mm_nn(Km.ld(par, m2, Vh), Wm.ld(par, m2, Vh)), Wm1), c);
+  const M3<R> Wp1 = Wm.ld(op, p1, Vh), Wm1 = Wm.ld(op, m1, Vh);
+  const R cr = (R)c;
+  M3<R> acc = Om.ld(par, h, Vh);
+  macc<R>(acc, tnn<R>(tnn<R>(Wp1, Wm.ld(par, p2, Vh)), Km.ld(par, h, Vh)), cr);
+  macc<R>(acc, tnn<R>(tnn<R>(Wp1, Km.ld(op, m1, Vh)), Wm1), cr);
+  macc<R>(acc, tnn<R>(tnn<R>(Km.ld(par, m2, Vh), Wm.ld(par, m2, Vh)), Wm1), cr);
   Om.st(par, h, Vh, acc);
 }
 
@@ -161,13 +179,17 @@ __global__ void __launch_bounds__(128) k_naik_adj(Geom g, const double2 *W, cons
 //   K_V = R K_W + (N + N^dag) V^dag,  M = K_W V,
 //   N = sum_i tr(M Q^i) Psi_i + f1 M + f2 (Q M + M Q),
 //   Psi_i = df_i/du R/2 + df_i/dv (u R - 1)/2 + df_i/dw (w/2) R^2.
-__global__ void __launch_bounds__(128) k_unit_adj(Geom g, const double2 *Vl, const double2 *KW, double2 *KV,
-                                                  unsigned int *nfilter) {
+// Always FP64 arithmetic (eigenvalues, 1/D); K_W and K_V stored in precision S.
+template <typename S>
+__global__ void __launch_bounds__(128) k_unit_adj(Geom g, const double2 *Vl, const typename Stor<S>::t *KW,
+                                                  typename Stor<S>::t *KV, unsigned int *nfilter) {
+  typedef typename Stor<S>::t T2;
   const int h = blockIdx.x * blockDim.x + threadIdx.x;
   const int par = blockIdx.y, mu = blockIdx.z;
   const int Vh = g.Vh;
   if (h >= Vh) return;
-  MatF Vm = link_dir((double2 *)Vl, mu, Vh), Kw = link_dir((double2 *)KW, mu, Vh), Kv = link_dir(KV, mu, Vh);
+  MatF Vm = link_dir((double2 *)Vl, mu, Vh);
+  MatT<S> Kw = link_dir((T2 *)KW, mu, Vh), Kv = link_dir(KV, mu, Vh);
   const M3<double> V = Vm.ld(par, h, Vh);
   M3<double> Q = mm_an(V, V), Q2 = mm_nn(Q, Q);
   double c0 = Q.e[0][0].re + Q.e[1][1].re + Q.e[2][2].re;
@@ -178,19 +200,19 @@ __global__ void __launch_bounds__(128) k_unit_adj(Geom g, const double2 *Vl, con
 #pragma unroll
     for (int k = 0; k < 3; k++) q3 += Q2.e[i][k].re * Q.e[k][i].re - Q2.e[i][k].im * Q.e[k][i].im;
   double c2 = q3 / 3, gv[3];
-  double S = c1 / 3 - c0 * (c0 / 18);
-  if (fabs(S) < 1.0e-14) {
+  double Sv = c1 / 3 - c0 * (c0 / 18);
+  if (fabs(Sv) < 1.0e-14) {
     gv[0] = gv[1] = gv[2] = c0 / 3;
   } else {
     double Rr = c2 / 2 - c0 * (c1 / 3) + c0 * c0 * (c0 / 27);
-    S = sqrt(S);
-    double RoS = Rr / (S * S * S), theta;
+    Sv = sqrt(Sv);
+    double RoS = Rr / (Sv * Sv * Sv), theta;
     if (!(fabs(RoS) < 1.0)) theta = Rr > 0 ? 0.0 : 3.14159265358979323846264338328;
     else theta = acos(RoS);
     double th3 = theta / 3, pi23 = 6.28318530717958647692528676656 / 3;
-    gv[0] = c0 / 3 + 2 * S * cos(th3);
-    gv[1] = c0 / 3 + 2 * S * cos(th3 + pi23);
-    gv[2] = c0 / 3 + 2 * S * cos(th3 + 2 * pi23);
+    gv[0] = c0 / 3 + 2 * Sv * cos(th3);
+    gv[1] = c0 / 3 + 2 * Sv * cos(th3 + pi23);
+    gv[2] = c0 / 3 + 2 * Sv * cos(th3 + 2 * pi23);
   }
   double gmin = fmin(gv[0], fmin(gv[1], gv[2]));
   if (gmin < 5.0e-5) {  // HISQ_FORCE_FILTER
@@ -223,7 +245,7 @@ __global__ void __launch_bounds__(128) k_unit_adj(Geom g, const double2 *Vl, con
       R.e[i][j].im = f1 * Q.e[i][j].im + f2 * Q2.e[i][j].im;
     }
   const M3<double> R2 = mm_nn(R, R);
-  const M3<double> Kwv = Kw.ld(par, h, Vh);
+  const M3<double> Kwv = to64<S>(Kw.ld(par, h, Vh));
   const M3<double> M = mm_nn(Kwv, V);
   const M3<double> QM = mm_nn(Q, M), MQ = mm_nn(M, Q), MQ2 = mm_nn(M, Q2);
   cplx<double> tr[3] = {{0, 0}, {0, 0}, {0, 0}};
@@ -263,26 +285,22 @@ __global__ void __launch_bounds__(128) k_unit_adj(Geom g, const double2 *Vl, con
       Nh.e[i][j].im = N.e[i][j].im - N.e[j][i].im;
     }
   M3<double> out = mm_nn(R, Kwv);
-  macc(out, mm_na(Nh, V), 1.0);
-  Kv.st(par, h, Vh, out);
-}
-
-// y = a x + b y over n double2
-__global__ void k_axpby(const double2 *x, double2 *y, double a, double b, size_t n) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    double2 u = x[i], v = y[i];
-    y[i] = make_double2(a * u.x + b * v.x, a * u.y + b * v.y);
-  }
+  macc<double>(out, mm_na(Nh, V), 1.0);
+  Kv.st(par, h, Vh, from64<S>(out));
 }
 
 // 5. mom <- TA(mom + fac U K_U) in MILC's anti_hermitmat layout, device AoS [V][4][10]
-__global__ void __launch_bounds__(128) k_force_mom(Geom g, const double2 *U, const double2 *KU, double *mom, double fac) {
+template <typename S>
+__global__ void __launch_bounds__(128) k_force_mom(Geom g, const double2 *U, const typename Stor<S>::t *KU,
+                                                   double *mom, double fac) {
+  typedef typename Stor<S>::t T2;
   const int h = blockIdx.x * blockDim.x + threadIdx.x;
   const int par = blockIdx.y, mu = blockIdx.z;
   const int Vh = g.Vh;
   if (h >= Vh) return;
-  MatF Um = link_dir((double2 *)U, mu, Vh), Km = link_dir((double2 *)KU, mu, Vh);
-  const M3<double> G = mm_nn(Um.ld(par, h, Vh), Km.ld(par, h, Vh));
+  MatF Um = link_dir((double2 *)U, mu, Vh);
+  MatT<S> Km = link_dir((T2 *)KU, mu, Vh);
+  const M3<double> G = mm_nn(Um.ld(par, h, Vh), to64<S>(Km.ld(par, h, Vh)));
   double *m = mom + (((size_t)par * Vh + h) * 4 + mu) * 10;
   // uncompress, add, compress (libraries/uncmp_ahmat.c, make_ahmat.c)
   double a01r = m[0], a01i = m[1], a02r = m[2], a02i = m[3], a12r = m[4], a12i = m[5];
@@ -300,214 +318,284 @@ __global__ void __launch_bounds__(128) k_force_mom(Geom g, const double2 *U, con
 struct ForceCoeffs { double one_link, naik, three_staple, five_staple, seven_staple, lepage; };
 
 static double g_force_flops = 0.0;
+static unsigned int g_nfilter = 0;
 
-static int staple_fwd(int mu, int nu, MatF Unu, MatF A, MatF S) {
-  Context &c = ctx();
-  MatF none = {nullptr, 0};
-  timing_begin(MKS_K_FORCE);
-  if (c.md_prec == MKS_PREC_SINGLE)
-    k_staple<float><<<dim3(grid_for(c.Vh, 128), 2), 128, 0, c.stream>>>(c.geom, mu, nu, Unu, A, none, 0.0, S);
-  else
-    k_staple<double><<<dim3(grid_for(c.Vh, 128), 2), 128, 0, c.stream>>>(c.geom, mu, nu, Unu, A, none, 0.0, S);
-  timing_end(MKS_K_FORCE);
-  g_force_flops += 4.0 * 198 * c.V;
-  MKS_CUDA(cudaGetLastError());
-  return MKS_OK;
-}
+// The force runs in the molecular-dynamics precision: FP64 fields and
+// arithmetic, or (MKS_PREC_SINGLE) every intermediate field -- the thin and
+// W links, the staples and all adjoints -- stored and multiplied in FP32.
+// The U(3)-projection adjoint keeps FP64 arithmetic and the momentum update
+// FP64 fields.
+template <typename R>
+struct ForceRun {
+  typedef typename Stor<R>::t T2;
 
-static int staple_adj(int mu, int nu, MatF Unu, MatF A, MatF K, double f, MatF KA, MatF KU) {
-  Context &c = ctx();
-  timing_begin(MKS_K_FORCE);
-  if (c.md_prec == MKS_PREC_SINGLE)
-    k_staple_adj<float><<<dim3(grid_for(c.Vh, 128), 2), 128, 0, c.stream>>>(c.geom, mu, nu, Unu, A, K, f, KA, KU);
-  else
-    k_staple_adj<double><<<dim3(grid_for(c.Vh, 128), 2), 128, 0, c.stream>>>(c.geom, mu, nu, Unu, A, K, f, KA, KU);
-  timing_end(MKS_K_FORCE);
-  g_force_flops += 12.0 * 198 * c.V;
-  MKS_CUDA(cudaGetLastError());
-  return MKS_OK;
-}
+  static int staple_fwd(int mu, int nu, MatT<R> Unu, MatT<R> A, MatT<R> S) {
+    Context &c = ctx();
+    MatT<R> none = {nullptr, 0};
+    timing_begin(MKS_K_FORCE);
+    k_staple<R><<<dim3(grid_for(c.Vh, 128), 2), 128, 0, c.stream>>>(c.geom, mu, nu, Unu, A, none, 0.0, S);
+    timing_end(MKS_K_FORCE);
+    g_force_flops += 4.0 * 198 * c.V;
+    MKS_CUDA(cudaGetLastError());
+    return MKS_OK;
+  }
 
-static int axpby(const double2 *x, double2 *y, double a, double b, size_t n) {
-  Context &c = ctx();
-  timing_begin(MKS_K_FORCE);
-  k_axpby<<<c.sm_count * 8, 256, 0, c.stream>>>(x, y, a, b, n);
-  timing_end(MKS_K_FORCE);
-  MKS_CUDA(cudaGetLastError());
-  return MKS_OK;
-}
+  static int staple_adj(int mu, int nu, MatT<R> Unu, MatT<R> A, MatT<R> K, double f, MatT<R> KA, MatT<R> KU) {
+    Context &c = ctx();
+    timing_begin(MKS_K_FORCE);
+    k_staple_adj<R><<<dim3(grid_for(c.Vh, 128), 2), 128, 0, c.stream>>>(c.geom, mu, nu, Unu, A, K, f, KA, KU);
+    timing_end(MKS_K_FORCE);
+    g_force_flops += 12.0 * 198 * c.V;
+    MKS_CUDA(cudaGetLastError());
+    return MKS_OK;
+  }
 
-// reverse of the fat-link staple recursion (load_fatlinks_cpu, ASQ_OPTIMIZED_FATTENING):
-// KU += d fat(links) / d links contracted with Kfat
-static int fat_adj(double2 *links, const ForceCoeffs &cf, double2 *Kfat, double2 *KU, double2 *S1, double2 *S2,
-                   double2 *K1, double2 *K2) {
-  Context &c = ctx();
-  const size_t Vh = c.Vh, nm = 2 * 9 * Vh;
-  const double one_link = cf.one_link - 6.0 * cf.lepage;
-  MKS_TRY(axpby(Kfat, KU, one_link, 1.0, 8 * 9 * Vh));
-  if (cf.three_staple == 0.0 && cf.lepage == 0.0 && cf.five_staple == 0.0) return MKS_OK;
-  const MatF mS1 = mat_field(S1, Vh), mS2 = mat_field(S2, Vh), mK1 = mat_field(K1, Vh), mK2 = mat_field(K2, Vh);
-  for (int mu = 0; mu < 4; mu++) {
-    const MatF Kd = link_dir(Kfat, mu, Vh), Um = link_dir(links, mu, Vh), KUm = link_dir(KU, mu, Vh);
-    // the fat link of direction mu as a [2][9][Vh] view: copy into K-scaled matrix fields below
-    for (int nu = 0; nu < 4; nu++) {
-      if (nu == mu) continue;
-      const MatF Un = link_dir(links, nu, Vh), KUn = link_dir(KU, nu, Vh);
-      MKS_TRY(staple_fwd(mu, nu, Un, Um, mS1));
-      // K1 = c3 Kfat_mu
-      MKS_CUDA(cudaMemsetAsync(K1, 0, nm * sizeof(double2), c.stream));
-      for (int p = 0; p < 2; p++)
-        MKS_TRY(axpby(Kd.p + p * Kd.ps, K1 + p * 9 * Vh, cf.three_staple, 1.0, 9 * Vh));
-      if (cf.lepage != 0.0) MKS_TRY(staple_adj(mu, nu, Un, mS1, Kd, cf.lepage, mK1, KUn));
-      for (int rho = 0; rho < 4; rho++) {
-        if (rho == mu || rho == nu) continue;
-        const MatF Ur = link_dir(links, rho, Vh), KUr = link_dir(KU, rho, Vh);
-        MKS_TRY(staple_fwd(mu, rho, Ur, mS1, mS2));
-        MKS_CUDA(cudaMemsetAsync(K2, 0, nm * sizeof(double2), c.stream));
+  static int axpby(const T2 *x, T2 *y, double a, double b, size_t n) {
+    Context &c = ctx();
+    timing_begin(MKS_K_FORCE);
+    k_axpby_t<T2><<<c.sm_count * 8, 256, 0, c.stream>>>(x, y, a, b, n);
+    timing_end(MKS_K_FORCE);
+    MKS_CUDA(cudaGetLastError());
+    return MKS_OK;
+  }
+
+  // reverse of the fat-link staple recursion (load_fatlinks_cpu, ASQ_OPTIMIZED_FATTENING):
+  // KU += d fat(links) / d links contracted with Kfat
+  static int fat_adj(T2 *links, const ForceCoeffs &cf, T2 *Kfat, T2 *KU, T2 *S1, T2 *S2, T2 *K1, T2 *K2) {
+    Context &c = ctx();
+    const size_t Vh = c.Vh, nm = 2 * 9 * Vh;
+    const double one_link = cf.one_link - 6.0 * cf.lepage;
+    MKS_TRY(axpby(Kfat, KU, one_link, 1.0, 8 * 9 * Vh));
+    if (cf.three_staple == 0.0 && cf.lepage == 0.0 && cf.five_staple == 0.0) return MKS_OK;
+    const MatT<R> mS1 = mat_field(S1, Vh), mS2 = mat_field(S2, Vh), mK1 = mat_field(K1, Vh), mK2 = mat_field(K2, Vh);
+    for (int mu = 0; mu < 4; mu++) {
+      const MatT<R> Kd = link_dir(Kfat, mu, Vh), Um = link_dir(links, mu, Vh), KUm = link_dir(KU, mu, Vh);
+      for (int nu = 0; nu < 4; nu++) {
+        if (nu == mu) continue;
+        const MatT<R> Un = link_dir(links, nu, Vh), KUn = link_dir(KU, nu, Vh);
+        MKS_TRY(staple_fwd(mu, nu, Un, Um, mS1));
+        // K1 = c3 Kfat_mu
+        MKS_CUDA(cudaMemsetAsync(K1, 0, nm * sizeof(T2), c.stream));
         for (int p = 0; p < 2; p++)
-          MKS_TRY(axpby(Kd.p + p * Kd.ps, K2 + p * 9 * Vh, cf.five_staple, 1.0, 9 * Vh));
-        for (int sig = 0; sig < 4; sig++) {
-          if (sig == mu || sig == nu || sig == rho) continue;
-          const MatF Us = link_dir(links, sig, Vh), KUs = link_dir(KU, sig, Vh);
-          MKS_TRY(staple_adj(mu, sig, Us, mS2, Kd, cf.seven_staple, mK2, KUs));
+          MKS_TRY(axpby(Kd.p + p * Kd.ps, K1 + p * 9 * Vh, cf.three_staple, 1.0, 9 * Vh));
+        if (cf.lepage != 0.0) MKS_TRY(staple_adj(mu, nu, Un, mS1, Kd, cf.lepage, mK1, KUn));
+        for (int rho = 0; rho < 4; rho++) {
+          if (rho == mu || rho == nu) continue;
+          const MatT<R> Ur = link_dir(links, rho, Vh), KUr = link_dir(KU, rho, Vh);
+          MKS_TRY(staple_fwd(mu, rho, Ur, mS1, mS2));
+          MKS_CUDA(cudaMemsetAsync(K2, 0, nm * sizeof(T2), c.stream));
+          for (int p = 0; p < 2; p++)
+            MKS_TRY(axpby(Kd.p + p * Kd.ps, K2 + p * 9 * Vh, cf.five_staple, 1.0, 9 * Vh));
+          for (int sig = 0; sig < 4; sig++) {
+            if (sig == mu || sig == nu || sig == rho) continue;
+            const MatT<R> Us = link_dir(links, sig, Vh), KUs = link_dir(KU, sig, Vh);
+            MKS_TRY(staple_adj(mu, sig, Us, mS2, Kd, cf.seven_staple, mK2, KUs));
+          }
+          MKS_TRY(staple_adj(mu, rho, Ur, mS1, mK2, 1.0, mK1, KUr));
         }
-        MKS_TRY(staple_adj(mu, rho, Ur, mS1, mK2, 1.0, mK1, KUr));
+        MKS_TRY(staple_adj(mu, nu, Un, Um, mK1, 1.0, KUm, KUn));
       }
-      MKS_TRY(staple_adj(mu, nu, Un, Um, mK1, 1.0, KUm, KUn));
+    }
+    return MKS_OK;
+  }
+
+  static int naik_adj(const T2 *W, const T2 *Kl, T2 *KW, double cn) {
+    Context &c = ctx();
+    timing_begin(MKS_K_FORCE);
+    k_naik_adj<R><<<dim3(grid_for(c.Vh, 128), 2, 4), 128, 0, c.stream>>>(c.geom, W, Kl, KW, cn);
+    timing_end(MKS_K_FORCE);
+    g_force_flops += 4.0 * 6 * 198 * c.V;
+    MKS_CUDA(cudaGetLastError());
+    return MKS_OK;
+  }
+
+  static int outer(const OuterArgs<R> &a, T2 *Kf, T2 *Kl) {
+    Context &c = ctx();
+    timing_begin(MKS_K_FORCE);
+    k_outer<R><<<dim3(grid_for(c.Vh, 128), 2, 4), 128, 0, c.stream>>>(c.geom, a, Kf, Kl);
+    timing_end(MKS_K_FORCE);
+    MKS_CUDA(cudaGetLastError());
+    return MKS_OK;
+  }
+
+  template <typename TO, typename TI>
+  static int convert(const TI *x, TO *y, size_t n) {
+    Context &c = ctx();
+    timing_begin(MKS_K_FORCE);
+    k_convert<TO, TI><<<c.sm_count * 8, 256, 0, c.stream>>>(x, y, n);
+    timing_end(MKS_K_FORCE);
+    MKS_CUDA(cudaGetLastError());
+    return MKS_OK;
+  }
+
+  // the FP64 resident field in precision R: the field itself for FP64, else
+  // a converted copy at dst
+  static int field_r(double2 *src, T2 *dst, size_t n, T2 **out) {
+    if constexpr (sizeof(R) == 8) {
+      (void)dst; (void)n;
+      *out = src;
+      return MKS_OK;
+    } else {
+      MKS_TRY((convert<T2, double2>(src, dst, n)));
+      *out = dst;
+      return MKS_OK;
     }
   }
-  return MKS_OK;
-}
 
-static int naik_adj(const double2 *W, const double2 *Kl, double2 *KW, double cn) {
-  Context &c = ctx();
-  timing_begin(MKS_K_FORCE);
-  k_naik_adj<<<dim3(grid_for(c.Vh, 128), 2, 4), 128, 0, c.stream>>>(c.geom, W, Kl, KW, cn);
-  timing_end(MKS_K_FORCE);
-  g_force_flops += 4.0 * 6 * 198 * c.V;
-  MKS_CUDA(cudaGetLastError());
-  return MKS_OK;
-}
+  // K_U out: FP64 copy of the adjoint for ku_out, or the momentum update
+  static int finish(double eps, T2 *KU, double *mom_dev, double2 *ku_out, T2 *scratch_unused) {
+    Context &c = ctx();
+    const size_t nl = 8 * 9 * c.Vh;
+    (void)scratch_unused;
+    if (ku_out) {
+      if constexpr (sizeof(R) == 8) {
+        MKS_CUDA(cudaMemcpyAsync(ku_out, KU, nl * sizeof(double2), cudaMemcpyDeviceToDevice, c.stream));
+      } else {
+        MKS_TRY((convert<double2, T2>(KU, ku_out, nl)));
+      }
+      MKS_CUDA(cudaStreamSynchronize(c.stream));
+      return MKS_OK;
+    }
+    timing_begin(MKS_K_FORCE);
+    k_force_mom<R><<<dim3(grid_for(c.Vh, 128), 2, 4), 128, 0, c.stream>>>(c.geom, c.auxU, KU, mom_dev, 2.0 * eps);
+    timing_end(MKS_K_FORCE);
+    MKS_CUDA(cudaGetLastError());
+    MKS_CUDA(cudaStreamSynchronize(c.stream));
+    return MKS_OK;
+  }
 
-static int outer(const OuterArgs &a, double2 *Kf, double2 *Kl) {
-  Context &c = ctx();
-  timing_begin(MKS_K_FORCE);
-  k_outer<<<dim3(grid_for(c.Vh, 128), 2, 4), 128, 0, c.stream>>>(c.geom, a, Kf, Kl);
-  timing_end(MKS_K_FORCE);
-  MKS_CUDA(cudaGetLastError());
-  return MKS_OK;
-}
+  // force inputs in precision R: the FP64 SoA vectors themselves, or FP32 copies in xs32
+  static int inputs(double2 *const *xs, int nterms, T2 *xs32, OuterArgs<R> &oa) {
+    const size_t nv = 6 * ctx().Vh;
+    for (int j = 0; j < nterms; j++) {
+      if constexpr (sizeof(R) == 8) {
+        (void)xs32; (void)nv;
+        oa.x[j] = xs[j];
+      } else {
+        MKS_TRY((convert<T2, double2>(xs[j], xs32 + (size_t)j * nv, nv)));
+        oa.x[j] = xs32 + (size_t)j * nv;
+      }
+    }
+    return MKS_OK;
+  }
 
-static unsigned int g_nfilter = 0;
+  static int hisq(double eps, const double *residues, double2 *const *xs, int nterms, const int *orders, int n_naiks,
+                  double *mom_dev, double2 *ku_out) {
+    Context &c = ctx();
+    const size_t Vh = c.Vh, nl = 8 * 9 * Vh, nm = 2 * 9 * Vh;
+    const ForceCoeffs c1 = {1.0 / 8.0, 0.0, -1.0 / 16.0, 1.0 / 64.0, -1.0 / 384.0, 0.0};
+    const ForceCoeffs c2 = {1.0 / 8.0 + 2.0 * 6.0 / 16.0 + 1.0 / 8.0, -1.0 / 24.0, -1.0 / 16.0, 1.0 / 64.0,
+                            -1.0 / 384.0, -2.0 / 16.0};
+    const ForceCoeffs c3 = {1.0 / 8.0, -1.0 / 24.0, 0, 0, 0, 0};
+    const bool low = sizeof(R) < 8;
+    // Kf Kl KW KV KU, S1 S2 K1 K2, and in FP32 the U and W copies and the inputs
+    const size_t total = 5 * nl + 4 * nm + (low ? 2 * nl + (size_t)nterms * 6 * Vh : 0);
+    T2 *buf = nullptr;
+    MKS_TRY(dev_alloc((void **)&buf, total * sizeof(T2)));
+    T2 *Kf = buf, *Kl = Kf + nl, *KW = Kl + nl, *KV = KW + nl, *KU = KV + nl;
+    T2 *S1 = KU + nl, *S2 = S1 + nm, *K1 = S2 + nm, *K2 = K1 + nm;
+    T2 *Ucp = K2 + nm, *Wcp = Ucp + nl, *xs32 = Wcp + nl;
+    unsigned int *nfilt = nullptr;
+    int rc = MKS_OK;
+    do {
+      if ((rc = dev_alloc((void **)&nfilt, sizeof(unsigned int))) < 0) break;
+      cudaMemsetAsync(nfilt, 0, sizeof(unsigned int), c.stream);
+      cudaMemsetAsync(buf, 0, 5 * nl * sizeof(T2), c.stream);
+      T2 *U, *W;
+      if ((rc = field_r(c.auxU, Ucp, nl, &U)) < 0) break;
+      if ((rc = field_r(c.auxW, Wcp, nl, &W)) < 0) break;
+      OuterArgs<R> oa;
+      memset(&oa, 0, sizeof oa);
+      if ((rc = inputs(xs, nterms, xs32, oa)) < 0) break;
+      for (int j = 0; j < nterms; j++) oa.res[j] = residues[j];
+      // level 2 with every term (the Naik group-0 table covers all terms)
+      oa.j0 = 0; oa.j1 = nterms; oa.scale = 1.0;
+      if ((rc = outer(oa, Kf, Kl)) < 0) break;
+      if ((rc = fat_adj(W, c2, Kf, KW, S1, S2, K1, K2)) < 0) break;
+      if ((rc = naik_adj(W, Kl, KW, c2.naik)) < 0) break;
+      // Naik-epsilon groups: eps_g (1-link + Naik)(W) for their own terms
+      int off = orders[0];
+      for (int gi = 1; gi < n_naiks && rc >= 0; gi++) {
+        cudaMemsetAsync(Kf, 0, 2 * nl * sizeof(T2), c.stream);
+        oa.j0 = off; oa.j1 = off + orders[gi]; oa.scale = c.slots[gi].eps_naik;
+        off += orders[gi];
+        if ((rc = outer(oa, Kf, Kl)) < 0) break;
+        if ((rc = fat_adj(W, c3, Kf, KW, S1, S2, K1, K2)) < 0) break;
+        if ((rc = naik_adj(W, Kl, KW, c3.naik)) < 0) break;
+      }
+      if (rc < 0) break;
+      timing_begin(MKS_K_FORCE);
+      k_unit_adj<R><<<dim3(grid_for(Vh, 128), 2, 4), 128, 0, c.stream>>>(c.geom, c.auxV, KW, KV, nfilt);
+      timing_end(MKS_K_FORCE);
+      g_force_flops += 20.0 * 198 * c.V * 4;
+      if (cudaGetLastError() != cudaSuccess) { rc = MKS_ERR_CUDA; break; }
+      if ((rc = fat_adj(U, c1, KV, KU, S1, S2, K1, K2)) < 0) break;
+      if ((rc = finish(eps, KU, mom_dev, ku_out, nullptr)) < 0) break;
+      cudaMemcpyAsync(&g_nfilter, nfilt, sizeof(unsigned int), cudaMemcpyDeviceToHost, c.stream);
+      if (cudaStreamSynchronize(c.stream) != cudaSuccess) rc = MKS_ERR_CUDA;
+    } while (0);
+    dev_free(nfilt);
+    dev_free(buf);
+    return rc;
+  }
+
+  // asqtad (generic_ks/fermion_force_fn_multi.c:80-316): one smearing
+  // level, the fat and Naik links built from the thin links U with the
+  // tadpole-improved coefficients and no projection, so K_U is the fat-link
+  // adjoint plus the Naik adjoint of the level-0 outer products.
+  static int asqtad(double eps, const double *residues, double2 *const *xs, int nterms, double *mom_dev,
+                    double2 *ku_out) {
+    Context &c = ctx();
+    const size_t Vh = c.Vh, nl = 8 * 9 * Vh, nm = 2 * 9 * Vh;
+    g_nfilter = 0;
+    const double u2 = c.aux_u0 * c.aux_u0, u4 = u2 * u2, u6 = u4 * u2;
+    // asqtad_action.h with the tadpole division of ks_action_paths.c
+    const ForceCoeffs ca = {1.0 / 8.0 + 6.0 / 16.0 + 1.0 / 8.0, -1.0 / 24.0 / u2, -1.0 / 16.0 / u2, 1.0 / 64.0 / u4,
+                            -1.0 / 384.0 / u6, -1.0 / 16.0 / u4};
+    const bool low = sizeof(R) < 8;
+    const size_t total = 3 * nl + 4 * nm + (low ? nl + (size_t)nterms * 6 * Vh : 0);
+    T2 *buf = nullptr;
+    MKS_TRY(dev_alloc((void **)&buf, total * sizeof(T2)));
+    T2 *Kf = buf, *Kl = Kf + nl, *KU = Kl + nl;
+    T2 *S1 = KU + nl, *S2 = S1 + nm, *K1 = S2 + nm, *K2 = K1 + nm;
+    T2 *Ucp = K2 + nm, *xs32 = Ucp + nl;
+    int rc = MKS_OK;
+    do {
+      if (cudaMemsetAsync(buf, 0, 3 * nl * sizeof(T2), c.stream) != cudaSuccess) { rc = MKS_ERR_CUDA; break; }
+      T2 *U;
+      if ((rc = field_r(c.auxU, Ucp, nl, &U)) < 0) break;
+      OuterArgs<R> oa;
+      memset(&oa, 0, sizeof oa);
+      if ((rc = inputs(xs, nterms, xs32, oa)) < 0) break;
+      for (int j = 0; j < nterms; j++) oa.res[j] = residues[j];
+      oa.j0 = 0; oa.j1 = nterms; oa.scale = 1.0;
+      if ((rc = outer(oa, Kf, Kl)) < 0) break;
+      if ((rc = fat_adj(U, ca, Kf, KU, S1, S2, K1, K2)) < 0) break;
+      if ((rc = naik_adj(U, Kl, KU, ca.naik)) < 0) break;
+      rc = finish(eps, KU, mom_dev, ku_out, nullptr);
+    } while (0);
+    dev_free(buf);
+    return rc;
+  }
+};
 
 // mom_dev: momentum updated in place; or, with ku_out set, K_U itself
 // (dS = 2 Re sum tr(K_U dU), [2][4][9][Vh] SoA) is copied there and mom_dev
 // is not touched.
 int force_dev(double eps, const double *residues, double2 *const *xs, int nterms, const int *orders, int n_naiks,
               double *mom_dev, double2 *ku_out) {
-  Context &c = ctx();
-  const size_t Vh = c.Vh, nl = 8 * 9 * Vh, nm = 2 * 9 * Vh;
   g_force_flops = 0.0;
-  const ForceCoeffs c1 = {1.0 / 8.0, 0.0, -1.0 / 16.0, 1.0 / 64.0, -1.0 / 384.0, 0.0};
-  const ForceCoeffs c2 = {1.0 / 8.0 + 2.0 * 6.0 / 16.0 + 1.0 / 8.0, -1.0 / 24.0, -1.0 / 16.0, 1.0 / 64.0,
-                          -1.0 / 384.0, -2.0 / 16.0};
-  const ForceCoeffs c3 = {1.0 / 8.0, -1.0 / 24.0, 0, 0, 0, 0};
-  double2 *buf = nullptr;
-  const size_t total = 5 * nl + 4 * nm;
-  MKS_TRY(dev_alloc((void **)&buf, total * sizeof(double2)));
-  double2 *Kf = buf, *Kl = Kf + nl, *KW = Kl + nl, *KV = KW + nl, *KU = KV + nl;
-  double2 *S1 = KU + nl, *S2 = S1 + nm, *K1 = S2 + nm, *K2 = K1 + nm;
-  unsigned int *nfilt = nullptr;
-  int rc = MKS_OK;
-  do {
-    if ((rc = dev_alloc((void **)&nfilt, sizeof(unsigned int))) < 0) break;
-    cudaMemsetAsync(nfilt, 0, sizeof(unsigned int), c.stream);
-    cudaMemsetAsync(buf, 0, 5 * nl * sizeof(double2), c.stream);
-    OuterArgs oa;
-    memset(&oa, 0, sizeof oa);
-    for (int j = 0; j < nterms; j++) { oa.x[j] = xs[j]; oa.res[j] = residues[j]; }
-    // level 2 with every term (the Naik group-0 table covers all terms)
-    oa.j0 = 0; oa.j1 = nterms; oa.scale = 1.0;
-    if ((rc = outer(oa, Kf, Kl)) < 0) break;
-    if ((rc = fat_adj(c.auxW, c2, Kf, KW, S1, S2, K1, K2)) < 0) break;
-    if ((rc = naik_adj(c.auxW, Kl, KW, c2.naik)) < 0) break;
-    // Naik-epsilon groups: eps_g (1-link + Naik)(W) for their own terms
-    int off = orders[0];
-    for (int gi = 1; gi < n_naiks && rc >= 0; gi++) {
-      cudaMemsetAsync(Kf, 0, 2 * nl * sizeof(double2), c.stream);
-      oa.j0 = off; oa.j1 = off + orders[gi]; oa.scale = c.slots[gi].eps_naik;
-      off += orders[gi];
-      if ((rc = outer(oa, Kf, Kl)) < 0) break;
-      if ((rc = fat_adj(c.auxW, c3, Kf, KW, S1, S2, K1, K2)) < 0) break;
-      if ((rc = naik_adj(c.auxW, Kl, KW, c3.naik)) < 0) break;
-    }
-    if (rc < 0) break;
-    timing_begin(MKS_K_FORCE);
-    k_unit_adj<<<dim3(grid_for(Vh, 128), 2, 4), 128, 0, c.stream>>>(c.geom, c.auxV, KW, KV, nfilt);
-    timing_end(MKS_K_FORCE);
-    g_force_flops += 20.0 * 198 * c.V * 4;
-    if (cudaGetLastError() != cudaSuccess) { rc = MKS_ERR_CUDA; break; }
-    if ((rc = fat_adj(c.auxU, c1, KV, KU, S1, S2, K1, K2)) < 0) break;
-    if (ku_out) {
-      if (cudaMemcpyAsync(ku_out, KU, nl * sizeof(double2), cudaMemcpyDeviceToDevice, c.stream) != cudaSuccess)
-        rc = MKS_ERR_CUDA;
-      if (rc >= 0 && cudaStreamSynchronize(c.stream) != cudaSuccess) rc = MKS_ERR_CUDA;
-      break;
-    }
-    timing_begin(MKS_K_FORCE);
-    k_force_mom<<<dim3(grid_for(Vh, 128), 2, 4), 128, 0, c.stream>>>(c.geom, c.auxU, KU, mom_dev, 2.0 * eps);
-    timing_end(MKS_K_FORCE);
-    if (cudaGetLastError() != cudaSuccess) { rc = MKS_ERR_CUDA; break; }
-    cudaMemcpyAsync(&g_nfilter, nfilt, sizeof(unsigned int), cudaMemcpyDeviceToHost, c.stream);
-    if (cudaStreamSynchronize(c.stream) != cudaSuccess) rc = MKS_ERR_CUDA;
-  } while (0);
-  dev_free(nfilt);
-  dev_free(buf);
-  return rc;
+  if (ctx().md_prec == MKS_PREC_SINGLE)
+    return ForceRun<float>::hisq(eps, residues, xs, nterms, orders, n_naiks, mom_dev, ku_out);
+  return ForceRun<double>::hisq(eps, residues, xs, nterms, orders, n_naiks, mom_dev, ku_out);
 }
 
-// asqtad (generic_ks/fermion_force_fn_multi.c:80-316): one smearing
-// level, the fat and Naik links built from the thin links U with the
-// tadpole-improved coefficients and no projection, so K_U is the fat-link
-// adjoint plus the Naik adjoint of the level-0 outer products.
 int force_asqtad_dev(double eps, const double *residues, double2 *const *xs, int nterms, double *mom_dev,
                      double2 *ku_out) {
-  Context &c = ctx();
-  const size_t Vh = c.Vh, nl = 8 * 9 * Vh, nm = 2 * 9 * Vh;
   g_force_flops = 0.0;
-  g_nfilter = 0;
-  const double u2 = c.aux_u0 * c.aux_u0, u4 = u2 * u2, u6 = u4 * u2;
-  // asqtad_action.h with the tadpole division of ks_action_paths.c
-  const ForceCoeffs ca = {1.0 / 8.0 + 6.0 / 16.0 + 1.0 / 8.0, -1.0 / 24.0 / u2, -1.0 / 16.0 / u2, 1.0 / 64.0 / u4,
-                          -1.0 / 384.0 / u6, -1.0 / 16.0 / u4};
-  double2 *buf = nullptr;
-  MKS_TRY(dev_alloc((void **)&buf, (3 * nl + 4 * nm) * sizeof(double2)));
-  double2 *Kf = buf, *Kl = Kf + nl, *KU = Kl + nl;
-  double2 *S1 = KU + nl, *S2 = S1 + nm, *K1 = S2 + nm, *K2 = K1 + nm;
-  int rc = MKS_OK;
-  do {
-    if (cudaMemsetAsync(buf, 0, 3 * nl * sizeof(double2), c.stream) != cudaSuccess) { rc = MKS_ERR_CUDA; break; }
-    OuterArgs oa;
-    memset(&oa, 0, sizeof oa);
-    for (int j = 0; j < nterms; j++) { oa.x[j] = xs[j]; oa.res[j] = residues[j]; }
-    oa.j0 = 0; oa.j1 = nterms; oa.scale = 1.0;
-    if ((rc = outer(oa, Kf, Kl)) < 0) break;
-    if ((rc = fat_adj(c.auxU, ca, Kf, KU, S1, S2, K1, K2)) < 0) break;
-    if ((rc = naik_adj(c.auxU, Kl, KU, ca.naik)) < 0) break;
-    if (ku_out) {
-      if (cudaMemcpyAsync(ku_out, KU, nl * sizeof(double2), cudaMemcpyDeviceToDevice, c.stream) != cudaSuccess)
-        rc = MKS_ERR_CUDA;
-      if (rc >= 0 && cudaStreamSynchronize(c.stream) != cudaSuccess) rc = MKS_ERR_CUDA;
-      break;
-    }
-    timing_begin(MKS_K_FORCE);
-    k_force_mom<<<dim3(grid_for(Vh, 128), 2, 4), 128, 0, c.stream>>>(c.geom, c.auxU, KU, mom_dev, 2.0 * eps);
-    timing_end(MKS_K_FORCE);
-    if (cudaGetLastError() != cudaSuccess) { rc = MKS_ERR_CUDA; break; }
-    if (cudaStreamSynchronize(c.stream) != cudaSuccess) rc = MKS_ERR_CUDA;
-  } while (0);
-  dev_free(buf);
-  return rc;
+  if (ctx().md_prec == MKS_PREC_SINGLE)
+    return ForceRun<float>::asqtad(eps, residues, xs, nterms, mom_dev, ku_out);
+  return ForceRun<double>::asqtad(eps, residues, xs, nterms, mom_dev, ku_out);
 }
 
 // Host staging shared by the force entry points: xxx[j] (MILC AoS, both

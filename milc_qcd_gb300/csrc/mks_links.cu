@@ -12,7 +12,12 @@
 // The fattening follows the optimised staple recursion of
 // load_fatlinks_cpu (ASQ_OPTIMIZED_FATTENING): one generalised staple
 //   S(x) = U_nu(x) A(x+nu) U_nu(x+mu)^dag + U_nu(x-nu)^dag A(x-nu) U_nu(x-nu+mu)
-// per launch (generic/general_staple.c:42-140), FP64 throughout.
+// per launch (generic/general_staple.c:42-140).  FP64 fields and
+// arithmetic, except in the molecular-dynamics FP32 setting
+// (mks_md_precision): there the thin links are copied to FP32 and every
+// smearing stage is stored and multiplied in FP32; the U(3) projection keeps
+// FP64 arithmetic, and the resident V, W and the slots' fat / long links
+// stay FP64 fields (holding the FP32 results).
 //
 // All link fields use the SoA layout of mks_internal.cuh: [par][dir][9][Vh].
 #include <cmath>
@@ -25,33 +30,41 @@ namespace mks {
 
 
 // out = a * in (all four directions, both parities)
-__global__ void k_scale_links(const double2 *in, double2 *out, double a, size_t n) {
+template <typename T2>
+__global__ void k_scale_links(const T2 *in, T2 *out, double a, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    double2 v = in[i];
-    out[i] = make_double2(a * v.x, a * v.y);
+    typedef decltype(T2::x) E;
+    const E ae = (E)a;
+    T2 v = in[i];
+    out[i] = {ae * v.x, ae * v.y};
   }
 }
-// out = x + a * y
-__global__ void k_axpy_links(const double2 *x, const double2 *y, double2 *out, double a, size_t n) {
+// out = x + a * y, into an FP64 field
+template <typename T2>
+__global__ void k_axpy_links(const T2 *x, const T2 *y, double2 *out, double a, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    double2 u = x[i], v = y[i];
-    out[i] = make_double2(u.x + a * v.x, u.y + a * v.y);
+    T2 u = x[i], v = y[i];
+    out[i] = make_double2((double)u.x + a * (double)v.x, (double)u.y + a * (double)v.y);
   }
 }
 
 // L_mu(x) = coef * W_mu(x) W_mu(x+mu) W_mu(x+2mu)   (load_lnglinks: the Naik path)
-__global__ void __launch_bounds__(128) k_naik(Geom g, const double2 *W, double2 *lng, double coef) {
+template <typename R>
+__global__ void __launch_bounds__(128) k_naik(Geom g, const typename Stor<R>::t *W, typename Stor<R>::t *lng,
+                                              double coef) {
+  typedef typename Stor<R>::t T2;
   const int h = blockIdx.x * blockDim.x + threadIdx.x;
   const int par = blockIdx.y, mu = blockIdx.z;
   const int Vh = g.Vh;
   if (h >= Vh) return;
-  MatF Wm = link_dir((double2 *)W, mu, Vh), Lm = link_dir(lng, mu, Vh);
+  MatT<R> Wm = link_dir((T2 *)W, mu, Vh), Lm = link_dir(lng, mu, Vh);
   const int x1 = nbr(g, par, h, mu, 1), x2 = nbr(g, par, h, mu, 2);
-  M3<double> p = mm_nn(Wm.ld(par, h, Vh), mm_nn(Wm.ld(1 - par, x1, Vh), Wm.ld(par, x2, Vh)));
+  M3<R> p = tnn<R>(Wm.ld(par, h, Vh), tnn<R>(Wm.ld(1 - par, x1, Vh), Wm.ld(par, x2, Vh)));
+  const R c = (R)coef;
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
-    for (int j = 0; j < 3; j++) { p.e[i][j].re *= coef; p.e[i][j].im *= coef; }
+    for (int j = 0; j < 3; j++) { p.e[i][j].re *= c; p.e[i][j].im *= c; }
   Lm.st(par, h, Vh, p);
 }
 
@@ -118,72 +131,119 @@ __device__ void u3_unitarize(const M3<double> &V, M3<double> &W, unsigned int *n
   W = mm_nn(V, S2);
 }
 
-__global__ void __launch_bounds__(128) k_unitarize(Geom g, const double2 *Vl, double2 *W, unsigned int *nsvd) {
+// W = V (V^dag V)^(-1/2) for V stored in precision R, FP64 arithmetic; W
+// stored into W64 and (when given) Wr, V copied to V64 (when given)
+template <typename R>
+__global__ void __launch_bounds__(128) k_unitarize(Geom g, const typename Stor<R>::t *Vl, double2 *V64, double2 *W,
+                                                   typename Stor<R>::t *Wr, unsigned int *nsvd) {
+  typedef typename Stor<R>::t T2;
   const int h = blockIdx.x * blockDim.x + threadIdx.x;
   const int par = blockIdx.y, mu = blockIdx.z;
   if (h >= g.Vh) return;
-  MatF Vm = link_dir((double2 *)Vl, mu, g.Vh), Wm = link_dir(W, mu, g.Vh);
-  M3<double> w;
-  u3_unitarize(Vm.ld(par, h, g.Vh), w, nsvd);
+  MatT<R> Vm = link_dir((T2 *)Vl, mu, g.Vh);
+  MatF Wm = link_dir(W, mu, g.Vh);
+  M3<R> vr = Vm.ld(par, h, g.Vh);
+  M3<double> v, w;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) v.e[i][j] = {(double)vr.e[i][j].re, (double)vr.e[i][j].im};
+  u3_unitarize(v, w, nsvd);
   Wm.st(par, h, g.Vh, w);
+  if (V64) link_dir(V64, mu, g.Vh).st(par, h, g.Vh, v);
+  if (Wr) {
+    M3<R> wr;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) wr.e[i][j] = {(R)w.e[i][j].re, (R)w.e[i][j].im};
+    link_dir(Wr, mu, g.Vh).st(par, h, g.Vh, wr);
+  }
 }
 
 struct FatCoeffs { double one_link, naik, three_staple, five_staple, seven_staple, lepage; };
 
-static int launch_staple(int mu, int nu, MatF Unu, MatF A, MatF fat, double coef, MatF sout) {
-  Context &c = ctx();
-  timing_begin(MKS_K_LINKS);
-  if (c.md_prec == MKS_PREC_SINGLE)
-    k_staple<float><<<dim3(grid_for(c.Vh, 128), 2), 128, 0, c.stream>>>(c.geom, mu, nu, Unu, A, fat, coef, sout);
-  else
-    k_staple<double><<<dim3(grid_for(c.Vh, 128), 2), 128, 0, c.stream>>>(c.geom, mu, nu, Unu, A, fat, coef, sout);
-  timing_end(MKS_K_LINKS);
-  MKS_CUDA(cudaGetLastError());
-  return MKS_OK;
-}
+// the smearing stages with fields stored and multiplied in precision R
+template <typename R>
+struct Smear {
+  typedef typename Stor<R>::t T2;
 
-// load_fatlinks_cpu, ASQ_OPTIMIZED_FATTENING (fermion_links_fn_load_milc.c:207-253)
-static int fatten(double2 *links, const FatCoeffs &cf, double2 *fat, double2 *staple, double2 *tmp) {
-  Context &c = ctx();
-  size_t Vh = c.Vh, nall = 8 * 9 * Vh;
-  double one_link = cf.one_link - 6.0 * cf.lepage;
-  timing_begin(MKS_K_LINKS);
-  k_scale_links<<<c.sm_count * 8, 256, 0, c.stream>>>(links, fat, one_link, nall);
-  timing_end(MKS_K_LINKS);
-  MKS_CUDA(cudaGetLastError());
-  if (cf.three_staple == 0.0 && cf.lepage == 0.0 && cf.five_staple == 0.0) return MKS_OK;
-  MatF none = {nullptr, 0};
-  for (int mu = 0; mu < 4; mu++) {
-    MatF Fm = link_dir(fat, mu, Vh), Um = link_dir(links, mu, Vh);
-    for (int nu = 0; nu < 4; nu++) {
-      if (nu == mu) continue;
-      MatF Un = link_dir(links, nu, Vh);
-      MatF S = mat_field(staple, Vh), T = mat_field(tmp, Vh);
-      MKS_TRY(launch_staple(mu, nu, Un, Um, Fm, cf.three_staple, S));
-      if (cf.lepage != 0.0) MKS_TRY(launch_staple(mu, nu, Un, S, Fm, cf.lepage, none));
-      for (int rho = 0; rho < 4; rho++) {
-        if (rho == mu || rho == nu) continue;
-        MatF Ur = link_dir(links, rho, Vh);
-        MKS_TRY(launch_staple(mu, rho, Ur, S, Fm, cf.five_staple, T));
-        for (int sig = 0; sig < 4; sig++) {
-          if (sig == mu || sig == nu || sig == rho) continue;
-          MatF Us = link_dir(links, sig, Vh);
-          MKS_TRY(launch_staple(mu, sig, Us, T, Fm, cf.seven_staple, none));
+  static int launch_staple(int mu, int nu, MatT<R> Unu, MatT<R> A, MatT<R> fat, double coef, MatT<R> sout) {
+    Context &c = ctx();
+    timing_begin(MKS_K_LINKS);
+    k_staple<R><<<dim3(grid_for(c.Vh, 128), 2), 128, 0, c.stream>>>(c.geom, mu, nu, Unu, A, fat, coef, sout);
+    timing_end(MKS_K_LINKS);
+    MKS_CUDA(cudaGetLastError());
+    return MKS_OK;
+  }
+
+  // load_fatlinks_cpu, ASQ_OPTIMIZED_FATTENING (fermion_links_fn_load_milc.c:207-253)
+  static int fatten(T2 *links, const FatCoeffs &cf, T2 *fat, T2 *staple, T2 *tmp) {
+    Context &c = ctx();
+    size_t Vh = c.Vh, nall = 8 * 9 * Vh;
+    double one_link = cf.one_link - 6.0 * cf.lepage;
+    timing_begin(MKS_K_LINKS);
+    k_scale_links<T2><<<c.sm_count * 8, 256, 0, c.stream>>>(links, fat, one_link, nall);
+    timing_end(MKS_K_LINKS);
+    MKS_CUDA(cudaGetLastError());
+    if (cf.three_staple == 0.0 && cf.lepage == 0.0 && cf.five_staple == 0.0) return MKS_OK;
+    MatT<R> none = {nullptr, 0};
+    for (int mu = 0; mu < 4; mu++) {
+      MatT<R> Fm = link_dir(fat, mu, Vh), Um = link_dir(links, mu, Vh);
+      for (int nu = 0; nu < 4; nu++) {
+        if (nu == mu) continue;
+        MatT<R> Un = link_dir(links, nu, Vh);
+        MatT<R> S = mat_field(staple, Vh), T = mat_field(tmp, Vh);
+        MKS_TRY(launch_staple(mu, nu, Un, Um, Fm, cf.three_staple, S));
+        if (cf.lepage != 0.0) MKS_TRY(launch_staple(mu, nu, Un, S, Fm, cf.lepage, none));
+        for (int rho = 0; rho < 4; rho++) {
+          if (rho == mu || rho == nu) continue;
+          MatT<R> Ur = link_dir(links, rho, Vh);
+          MKS_TRY(launch_staple(mu, rho, Ur, S, Fm, cf.five_staple, T));
+          for (int sig = 0; sig < 4; sig++) {
+            if (sig == mu || sig == nu || sig == rho) continue;
+            MatT<R> Us = link_dir(links, sig, Vh);
+            MKS_TRY(launch_staple(mu, sig, Us, T, Fm, cf.seven_staple, none));
+          }
         }
       }
     }
+    return MKS_OK;
   }
-  return MKS_OK;
-}
 
-static int naik(double2 *W, double2 *lng, double coef) {
-  Context &c = ctx();
-  timing_begin(MKS_K_LINKS);
-  k_naik<<<dim3(grid_for(c.Vh, 128), 2, 4), 128, 0, c.stream>>>(c.geom, W, lng, coef);
-  timing_end(MKS_K_LINKS);
-  MKS_CUDA(cudaGetLastError());
-  return MKS_OK;
+  static int naik(T2 *W, T2 *lng, double coef) {
+    Context &c = ctx();
+    timing_begin(MKS_K_LINKS);
+    k_naik<R><<<dim3(grid_for(c.Vh, 128), 2, 4), 128, 0, c.stream>>>(c.geom, W, lng, coef);
+    timing_end(MKS_K_LINKS);
+    MKS_CUDA(cudaGetLastError());
+    return MKS_OK;
+  }
+
+  static int unitarize(T2 *Vl, double2 *V64, double2 *W, T2 *Wr, unsigned int *nsvd) {
+    Context &c = ctx();
+    timing_begin(MKS_K_LINKS);
+    k_unitarize<R><<<dim3(grid_for(c.Vh, 128), 2, 4), 128, 0, c.stream>>>(c.geom, Vl, V64, W, Wr, nsvd);
+    timing_end(MKS_K_LINKS);
+    MKS_CUDA(cudaGetLastError());
+    return MKS_OK;
+  }
+
+  static int to_f64(const T2 *x, double2 *y, size_t n) {
+    Context &c = ctx();
+    timing_begin(MKS_K_LINKS);
+    k_convert<double2, T2><<<c.sm_count * 8, 256, 0, c.stream>>>(x, y, n);
+    timing_end(MKS_K_LINKS);
+    MKS_CUDA(cudaGetLastError());
+    return MKS_OK;
+  }
+};
+
+// the FP64 entry points of the MILC-facing loaders
+static int fatten(double2 *links, const FatCoeffs &cf, double2 *fat, double2 *staple, double2 *tmp) {
+  return Smear<double>::fatten(links, cf, fat, staple, tmp);
 }
+static int naik(double2 *W, double2 *lng, double coef) { return Smear<double>::naik(W, lng, coef); }
 
 static unsigned int g_nsvd = 0;
 
@@ -199,14 +259,15 @@ int links_from_thin(int action, const double *thin_dev_aos, int n_naiks, const d
   return links_from_aux(action, n_naiks, eps_naik, u0);
 }
 
-// fat/long links of slots 0..n_naiks-1 built from the resident thin links auxU
-int links_from_aux(int action, int n_naiks, const double *eps_naik, double u0) {
+// fat/long links of slots 0..n_naiks-1 built from the resident thin links
+// auxU, smearing in precision R (the field pointers of the stages are the
+// resident FP64 fields for FP64, FP32 scratch copies otherwise)
+template <typename R>
+static int build_links(int action, int n_naiks, const double *eps_naik, double u0) {
+  typedef typename Stor<R>::t T2;
+  constexpr bool low = sizeof(R) < 8;
   Context &c = ctx();
   size_t Vh = c.Vh, nall = 8 * 9 * Vh;
-  if (!c.auxU) return MKS_ERR_STATE;
-  double2 *staple, *tmp, *f3 = nullptr, *l3 = nullptr;
-  MKS_TRY(dev_alloc((void **)&staple, 2 * 9 * Vh * sizeof(double2)));
-  MKS_TRY(dev_alloc((void **)&tmp, 2 * 9 * Vh * sizeof(double2)));
   for (int i = 0; i < n_naiks; i++) {
     LinkSlot &s = c.slots[i];
     if (!s.fat64) {
@@ -214,57 +275,87 @@ int links_from_aux(int action, int n_naiks, const double *eps_naik, double u0) {
       MKS_TRY(dev_alloc((void **)&s.lng64, nall * sizeof(double2)));
     }
   }
-  unsigned int *nsvd;
-  MKS_TRY(dev_alloc((void **)&nsvd, sizeof(unsigned int)));
-  MKS_CUDA(cudaMemsetAsync(nsvd, 0, sizeof(unsigned int), c.stream));
+  // staple, tmp; FP32: U, V, W, fat, long copies; Naik groups: f3, l3
+  const size_t nscr = 2 * 2 * 9 * Vh + (low ? 5 * nall : 0) + (n_naiks > 1 ? 2 * nall : 0);
+  T2 *scr = nullptr;
+  MKS_TRY(dev_alloc((void **)&scr, nscr * sizeof(T2)));
+  T2 *staple = scr, *tmp = staple + 2 * 9 * Vh, *p = tmp + 2 * 9 * Vh;
+  T2 *Ucp = nullptr, *Vcp = nullptr, *Wcp = nullptr, *Fcp = nullptr, *Lcp = nullptr, *f3 = nullptr, *l3 = nullptr;
+  if (low) { Ucp = p; Vcp = p + nall; Wcp = p + 2 * nall; Fcp = p + 3 * nall; Lcp = p + 4 * nall; p += 5 * nall; }
+  if (n_naiks > 1) { f3 = p; l3 = p + nall; }
+  unsigned int *nsvd = nullptr;
+  int rc = dev_alloc((void **)&nsvd, sizeof(unsigned int));
   LinkSlot &s0 = c.slots[0];
-  if (action == MKS_ACTION_HISQ) {
-    // generic_ks/imp_actions/hisq/hisq_u3_action.h: path_coeff_1 / _2 / _3 (no tadpole factors)
-    const FatCoeffs c1 = {1.0 / 8.0, 0.0, -1.0 / 16.0, 1.0 / 64.0, -1.0 / 384.0, 0.0};
-    const FatCoeffs c2 = {1.0 / 8.0 + 2.0 * 6.0 / 16.0 + 1.0 / 8.0, -1.0 / 24.0, -1.0 / 16.0, 1.0 / 64.0,
-                          -1.0 / 384.0, -2.0 / 16.0};
-    const FatCoeffs c3 = {1.0 / 8.0, -1.0 / 24.0, 0, 0, 0, 0};
-    MKS_TRY(fatten(c.auxU, c1, c.auxV, staple, tmp));
-    timing_begin(MKS_K_LINKS);
-    k_unitarize<<<dim3(grid_for(Vh, 128), 2, 4), 128, 0, c.stream>>>(c.geom, c.auxV, c.auxW, nsvd);
-    timing_end(MKS_K_LINKS);
-    MKS_CUDA(cudaGetLastError());
-    MKS_TRY(fatten(c.auxW, c2, s0.fat64, staple, tmp));
-    MKS_TRY(naik(c.auxW, s0.lng64, c2.naik));
-    if (n_naiks > 1) {
-      MKS_TRY(dev_alloc((void **)&f3, nall * sizeof(double2)));
-      MKS_TRY(dev_alloc((void **)&l3, nall * sizeof(double2)));
-      MKS_TRY(fatten(c.auxW, c3, f3, staple, tmp));
-      MKS_TRY(naik(c.auxW, l3, c3.naik));
-      for (int i = 1; i < n_naiks; i++) {
-        LinkSlot &s = c.slots[i];
-        k_axpy_links<<<c.sm_count * 8, 256, 0, c.stream>>>(s0.fat64, f3, s.fat64, eps_naik[i], nall);
-        k_axpy_links<<<c.sm_count * 8, 256, 0, c.stream>>>(s0.lng64, l3, s.lng64, eps_naik[i], nall);
-        c.launches += 2;
-      }
+  typedef Smear<R> Sm;
+  do {
+    if (rc < 0) break;
+    if (cudaMemsetAsync(nsvd, 0, sizeof(unsigned int), c.stream) != cudaSuccess) { rc = MKS_ERR_CUDA; break; }
+    T2 *U = (T2 *)c.auxU;
+    if constexpr (low) {
+      timing_begin(MKS_K_LINKS);
+      k_convert<T2, double2><<<c.sm_count * 8, 256, 0, c.stream>>>(c.auxU, Ucp, nall);
+      timing_end(MKS_K_LINKS);
+      U = Ucp;
     }
-  } else {
-    // asqtad_action.h with the tadpole division of ks_action_paths.c
-    const double u2 = u0 * u0, u4 = u2 * u2, u6 = u4 * u2;
-    const FatCoeffs ca = {1.0 / 8.0 + 6.0 / 16.0 + 1.0 / 8.0, -1.0 / 24.0 / u2, -1.0 / 16.0 / u2, 1.0 / 64.0 / u4,
-                          -1.0 / 384.0 / u6, -1.0 / 16.0 / u4};
-    MKS_TRY(fatten(c.auxU, ca, s0.fat64, staple, tmp));
-    MKS_TRY(naik(c.auxU, s0.lng64, ca.naik));
-    n_naiks = 1;
-  }
-  for (int i = 0; i < n_naiks; i++) {
-    LinkSlot &s = c.slots[i];
-    MKS_TRY(links_make_lowprec(s));
-    s.eps_naik = eps_naik ? eps_naik[i] : 0.0;
-    s.valid = true;
-  }
-  c.aux_action = action;
-  c.aux_u0 = u0;
-  c.links_prec = c.md_prec;
-  MKS_CUDA(cudaMemcpyAsync(&g_nsvd, nsvd, sizeof(unsigned int), cudaMemcpyDeviceToHost, c.stream));
-  MKS_CUDA(cudaStreamSynchronize(c.stream));
-  dev_free(nsvd); dev_free(staple); dev_free(tmp); dev_free(f3); dev_free(l3);
-  return MKS_OK;
+    T2 *F = low ? Fcp : (T2 *)s0.fat64, *L = low ? Lcp : (T2 *)s0.lng64;
+    if (action == MKS_ACTION_HISQ) {
+      // generic_ks/imp_actions/hisq/hisq_u3_action.h: path_coeff_1 / _2 / _3 (no tadpole factors)
+      const FatCoeffs c1 = {1.0 / 8.0, 0.0, -1.0 / 16.0, 1.0 / 64.0, -1.0 / 384.0, 0.0};
+      const FatCoeffs c2 = {1.0 / 8.0 + 2.0 * 6.0 / 16.0 + 1.0 / 8.0, -1.0 / 24.0, -1.0 / 16.0, 1.0 / 64.0,
+                            -1.0 / 384.0, -2.0 / 16.0};
+      const FatCoeffs c3 = {1.0 / 8.0, -1.0 / 24.0, 0, 0, 0, 0};
+      T2 *Vf = low ? Vcp : (T2 *)c.auxV, *W = low ? Wcp : (T2 *)c.auxW;
+      if ((rc = Sm::fatten(U, c1, Vf, staple, tmp)) < 0) break;
+      if ((rc = Sm::unitarize(Vf, low ? c.auxV : nullptr, c.auxW, low ? Wcp : nullptr, nsvd)) < 0) break;
+      if ((rc = Sm::fatten(W, c2, F, staple, tmp)) < 0) break;
+      if ((rc = Sm::naik(W, L, c2.naik)) < 0) break;
+      if (n_naiks > 1) {
+        if ((rc = Sm::fatten(W, c3, f3, staple, tmp)) < 0) break;
+        if ((rc = Sm::naik(W, l3, c3.naik)) < 0) break;
+        for (int i = 1; i < n_naiks; i++) {
+          LinkSlot &s = c.slots[i];
+          k_axpy_links<T2><<<c.sm_count * 8, 256, 0, c.stream>>>(F, f3, s.fat64, eps_naik[i], nall);
+          k_axpy_links<T2><<<c.sm_count * 8, 256, 0, c.stream>>>(L, l3, s.lng64, eps_naik[i], nall);
+          c.launches += 2;
+        }
+      }
+    } else {
+      // asqtad_action.h with the tadpole division of ks_action_paths.c
+      const double u2 = u0 * u0, u4 = u2 * u2, u6 = u4 * u2;
+      const FatCoeffs ca = {1.0 / 8.0 + 6.0 / 16.0 + 1.0 / 8.0, -1.0 / 24.0 / u2, -1.0 / 16.0 / u2, 1.0 / 64.0 / u4,
+                            -1.0 / 384.0 / u6, -1.0 / 16.0 / u4};
+      if ((rc = Sm::fatten(U, ca, F, staple, tmp)) < 0) break;
+      if ((rc = Sm::naik(U, L, ca.naik)) < 0) break;
+      n_naiks = 1;
+    }
+    if constexpr (low) {
+      if ((rc = Sm::to_f64(F, s0.fat64, nall)) < 0) break;
+      if ((rc = Sm::to_f64(L, s0.lng64, nall)) < 0) break;
+    }
+    for (int i = 0; i < n_naiks && rc >= 0; i++) {
+      LinkSlot &s = c.slots[i];
+      rc = links_make_lowprec(s);
+      s.eps_naik = eps_naik ? eps_naik[i] : 0.0;
+      s.valid = true;
+    }
+    if (rc < 0) break;
+    c.aux_action = action;
+    c.aux_u0 = u0;
+    c.links_prec = low ? MKS_PREC_SINGLE : MKS_PREC_DOUBLE;
+    if (cudaMemcpyAsync(&g_nsvd, nsvd, sizeof(unsigned int), cudaMemcpyDeviceToHost, c.stream) != cudaSuccess)
+      rc = MKS_ERR_CUDA;
+    if (rc >= 0 && cudaStreamSynchronize(c.stream) != cudaSuccess) rc = MKS_ERR_CUDA;
+  } while (0);
+  cudaStreamSynchronize(c.stream);
+  dev_free(nsvd);
+  dev_free(scr);
+  return rc;
+}
+
+int links_from_aux(int action, int n_naiks, const double *eps_naik, double u0) {
+  if (!ctx().auxU) return MKS_ERR_STATE;
+  if (ctx().md_prec == MKS_PREC_SINGLE) return build_links<float>(action, n_naiks, eps_naik, u0);
+  return build_links<double>(action, n_naiks, eps_naik, u0);
 }
 
 }  // namespace mks
@@ -395,12 +486,7 @@ int mks_hisq_aux_links(const double coeffs1[6], const double *U, double *V, doub
   c.aux_action = MKS_ACTION_HISQ;
   c.aux_u0 = 1.0;
   if (rc >= 0) rc = fatten(c.auxU, cf, c.auxV, S, T);
-  if (rc >= 0) {
-    timing_begin(MKS_K_LINKS);
-    k_unitarize<<<dim3(grid_for(Vh, 128), 2, 4), 128, 0, c.stream>>>(c.geom, c.auxV, c.auxW, nsvd);
-    timing_end(MKS_K_LINKS);
-    if (cudaGetLastError() != cudaSuccess) rc = MKS_ERR_CUDA;
-  }
+  if (rc >= 0) rc = Smear<double>::unitarize(c.auxV, nullptr, c.auxW, nullptr, nsvd);
   if (rc >= 0 && cudaMemcpyAsync(&g_nsvd, nsvd, sizeof(unsigned int), cudaMemcpyDeviceToHost, c.stream) != cudaSuccess)
     rc = MKS_ERR_CUDA;
   if (rc >= 0 && V) rc = to_host(c.auxV, V, stage);

@@ -921,6 +921,10 @@ static int poll_interval() {
 // Solve (sigma_s - D_par D_opar) x_s = src_s on parity par for nsrc sources
 // held in FP64 SoA device fields f.src/f.x (x = initial guess on entry);
 // sigma_s = 4 m^2 for a plain mass, or a multi-shift offset when refining.
+// Sources leave the block when they finish: the device state array and the
+// field pointers passed to the kernels hold only the running sources
+// (act[k] = original index of block position k), so a source that has
+// converged costs no D_eo work while the others continue.
 static int block_cg_shifted(int slot, int par, int nsrc, const double *msq4, const mks_invert_arg *arg,
                             CgFields &f, mks_invert_result *res) {
   Context &c = ctx();
@@ -931,8 +935,9 @@ static int block_cg_shifted(int slot, int par, int nsrc, const double *msq4, con
   MKS_TRY(wsv("cg_state", MAXSRC, &S.st));
   MKS_TRY(wsv("cg_skip", 1, &S.skip));
 
+  std::vector<CgState> fin(nsrc);   // final state by original index
+  std::vector<int> act, xzero;      // running sources; zero initial guess by block position
   // source norms and initial-guess norms (a zero guess needs no D D x)
-  std::vector<int> xzero(nsrc, 0);
   {
     OpNorm<double2> op;
     memset(&op, 0, sizeof op);
@@ -944,11 +949,9 @@ static int block_cg_shifted(int slot, int par, int nsrc, const double *msq4, con
     std::vector<double> h(2 * nsrc);
     MKS_CUDA(cudaMemcpyAsync(h.data(), tot, 2 * nsrc * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     MKS_CUDA(cudaStreamSynchronize(c.stream));
-    for (int s = 0; s < nsrc; s++) xzero[s] = h[nsrc + s] == 0.0;
-    std::vector<CgState> hs(nsrc);
-    memset(hs.data(), 0, nsrc * sizeof(CgState));
     for (int s = 0; s < nsrc; s++) {
-      CgState &q = hs[s];
+      CgState &q = fin[s];
+      memset(&q, 0, sizeof q);
       q.source_norm = h[s];
       q.rsqmin = arg->resid * arg->resid;
       q.relrsqmin = arg->relresid * arg->relresid;
@@ -960,56 +963,84 @@ static int block_cg_shifted(int slot, int par, int nsrc, const double *msq4, con
       q.size_relr = 1.0;
       q.converged = 1;
       q.status = ST_HOST;
-      if (h[s] == 0.0) q.status = ST_DONE;  // trivial source: zero solution
+      if (h[s] == 0.0) {
+        q.status = ST_DONE;  // trivial source: zero solution
+        MKS_CUDA(cudaMemsetAsync(f.x[s], 0, 3 * c.Vh * sizeof(double2), c.stream));
+      } else {
+        act.push_back(s);
+        xzero.push_back(h[nsrc + s] == 0.0);
+      }
     }
-    MKS_TRY(write_states(S, nsrc, hs.data(), 1));
-    for (int s = 0; s < nsrc; s++)
-      if (h[s] == 0.0) MKS_CUDA(cudaMemsetAsync(f.x[s], 0, 3 * c.Vh * sizeof(double2), c.stream));
   }
-  if (mixed) {
+  // block view of the running sources
+  CgFields g;
+  double sig[MAXSRC];
+  std::vector<CgState> hs;
+  auto compact = [&](const std::vector<int> &keep) {
+    std::vector<int> a2;
+    std::vector<CgState> h2;
+    for (int k : keep) { a2.push_back(act[k]); h2.push_back(hs.empty() ? fin[act[k]] : hs[k]); }
+    act.swap(a2);
+    hs.swap(h2);
+    memset(&g, 0, sizeof g);
+    for (int k = 0; k < (int)act.size(); k++) {
+      const int s = act[k];
+      g.src[k] = f.src[s]; g.x[k] = f.x[s]; g.r[k] = f.r[s]; g.p[k] = f.p[s]; g.ttt[k] = f.ttt[s]; g.t[k] = f.t[s];
+      g.x32[k] = f.x32[s]; g.r32[k] = f.r32[s]; g.p32[k] = f.p32[s]; g.ttt32[k] = f.ttt32[s]; g.t32[k] = f.t32[s];
+      g.p16[k] = f.p16[s]; g.t16[k] = f.t16[s]; g.p16n[k] = f.p16n[s]; g.t16n[k] = f.t16n[s];
+      sig[k] = msq4[s];
+    }
+  };
+  {
+    std::vector<int> all(act.size());
+    for (int k = 0; k < (int)all.size(); k++) all[k] = k;
+    compact(all);
+  }
+  int nact = (int)act.size();
+  if (nact > 0) MKS_TRY(write_states(S, nact, hs.data(), 1));
+  if (mixed && nact > 0) {
     OpZero<float2> z;
-    for (int s = 0; s < nsrc; s++) z.v[s] = f.x32[s];
+    for (int k = 0; k < nact; k++) z.v[k] = g.x32[k];
     z.Vh = (int)c.Vh;
-    MKS_TRY((launch_site<OpZero<float2>, 0, FinNone>(MKS_K_BLAS, z, FinNone(), nullptr, nsrc)));
+    MKS_TRY((launch_site<OpZero<float2>, 0, FinNone>(MKS_K_BLAS, z, FinNone(), nullptr, nact)));
   }
-  std::vector<CgState> hs(nsrc);
   bool first = true;
   int guard = 0;
-  while (true) {
-    MKS_TRY(read_states(S, nsrc, hs.data()));
+  while (nact > 0) {
+    MKS_TRY(read_states(S, nact, hs.data()));
     bool any_host = false, any_run = false;
-    for (int s = 0; s < nsrc; s++) {
-      any_host |= hs[s].status == ST_HOST;
-      any_run |= hs[s].status == ST_RUN;
+    for (int k = 0; k < nact; k++) {
+      any_host |= hs[k].status == ST_HOST;
+      any_run |= hs[k].status == ST_RUN;
     }
     if (any_host) {
       // restart (FP64 CG) or reliable update (mixed): recompute the true residual
       if (mixed && !first) {
         OpAccumX ax;
         memset(&ax, 0, sizeof ax);
-        for (int s = 0; s < nsrc; s++) { ax.x64[s] = f.x[s]; ax.x32[s] = f.x32[s]; }
+        for (int k = 0; k < nact; k++) { ax.x64[k] = g.x[k]; ax.x32[k] = g.x32[k]; }
         ax.st = S.st; ax.Vh = (int)c.Vh;
-        MKS_TRY((launch_site<OpAccumX, 0, FinNone>(MKS_K_BLAS, ax, FinNone(), nullptr, nsrc)));
+        MKS_TRY((launch_site<OpAccumX, 0, FinNone>(MKS_K_BLAS, ax, FinNone(), nullptr, nact)));
       }
       std::vector<double> relrsq;
-      std::vector<int> need(nsrc);
-      for (int s = 0; s < nsrc; s++) need[s] = hs[s].status == ST_HOST;
-      MKS_TRY(true_residual(sl, par, nsrc, msq4, f, S, mixed ? (first ? 1 : 0) : 1, need,
-                            first ? xzero : std::vector<int>(nsrc, 0), arg->relresid > 0 ? &relrsq : nullptr));
+      std::vector<int> need(nact);
+      for (int k = 0; k < nact; k++) need[k] = hs[k].status == ST_HOST;
+      MKS_TRY(true_residual(sl, par, nact, sig, g, S, mixed ? (first ? 1 : 0) : 1, need,
+                            first ? xzero : std::vector<int>(nact, 0), arg->relresid > 0 ? &relrsq : nullptr));
       if (mixed) {
         OpDemote dm;
         memset(&dm, 0, sizeof dm);
-        for (int s = 0; s < nsrc; s++) {
-          dm.r64[s] = f.r[s]; dm.r32[s] = f.r32[s]; dm.p32[s] = f.p32[s]; dm.p16[s] = f.p16[s]; dm.p16n[s] = f.p16n[s];
+        for (int k = 0; k < nact; k++) {
+          dm.r64[k] = g.r[k]; dm.r32[k] = g.r32[k]; dm.p32[k] = g.p32[k]; dm.p16[k] = g.p16[k]; dm.p16n[k] = g.p16n[k];
         }
         dm.st = S.st; dm.Vh = (int)c.Vh; dm.setp = first ? 1 : 0;
-        MKS_TRY((launch_site<OpDemote, 0, FinNone>(MKS_K_BLAS, dm, FinNone(), nullptr, nsrc)));
+        MKS_TRY((launch_site<OpDemote, 0, FinNone>(MKS_K_BLAS, dm, FinNone(), nullptr, nact)));
       }
-      MKS_TRY(read_states(S, nsrc, hs.data()));
-      for (int s = 0; s < nsrc; s++) {
-        CgState &q = hs[s];
+      MKS_TRY(read_states(S, nact, hs.data()));
+      for (int k = 0; k < nact; k++) {
+        CgState &q = hs[k];
         if (q.status != ST_HOST) continue;
-        if (!relrsq.empty()) q.final_relrsq = relrsq[s] * relrsq[s];
+        if (!relrsq.empty()) q.final_relrsq = relrsq[k] * relrsq[k];
         bool ok = (q.rsqmin <= 0 || q.rsqmin > q.final_rsq) &&
                   (q.relrsqmin <= 0 || q.relrsqmin > q.final_relrsq);
         if (mixed) {
@@ -1032,20 +1063,28 @@ static int block_cg_shifted(int slot, int par, int nsrc, const double *msq4, con
         }
       }
       first = false;
-      any_run = false;
-      for (int s = 0; s < nsrc; s++) any_run |= hs[s].status == ST_RUN;
-      MKS_TRY(write_states(S, nsrc, hs.data(), 0));
+      std::vector<int> keep;
+      for (int k = 0; k < nact; k++) {
+        if (hs[k].status == ST_DONE) fin[act[k]] = hs[k];
+        else keep.push_back(k);
+      }
+      if ((int)keep.size() < nact) {
+        compact(keep);
+        nact = (int)act.size();
+      }
+      any_run = nact > 0;
+      if (nact > 0) MKS_TRY(write_states(S, nact, hs.data(), 0));
     }
     if (!any_run) break;
     int np = poll_interval();
-    MKS_TRY(run_batch(sl, par, nsrc, prec, msq4, f, S, np));
+    MKS_TRY(run_batch(sl, par, nact, prec, sig, g, S, np));
     if (++guard > 10000000) return MKS_ERR_TIMEOUT;
   }
-  if (mixed) {
-    // x64 already holds the accumulated solution: the last reliable update folded x32 in
-  }
+  for (int k = 0; k < nact; k++) fin[act[k]] = hs[k];
+  // mixed precision: x64 already holds the accumulated solution (the last
+  // reliable update folded x32 in)
   for (int s = 0; s < nsrc; s++) {
-    CgState &q = hs[s];
+    const CgState &q = fin[s];
     mks_invert_result &o = res[s];
     o.final_rsq = q.final_rsq;
     o.final_relrsq = q.final_relrsq;
@@ -1402,7 +1441,11 @@ struct MsState {
   double rsq, pkp, source_norm, rsqstop, shift0;
   double shifts[MAXSH], zeta_i[MAXSH], zeta_im1[MAXSH], zeta_ip1[MAXSH];
   double beta_i[MAXSH], beta_im1[MAXSH], alpha[MAXSH];
-  int iter, niter, status, j_low, num_now, num_offsets, need_scroll, pad;
+  double maxrr, delta;   // reliable updates of the sloppy solve: max |r| since the last one, threshold
+  double rsqretire;      // sloppy solve: a shift whose |zeta_j r|^2 fell below this is no longer updated
+  int iter, niter, status, j_low, num_now, num_offsets, need_scroll, want_reliable;
+  int n_reliable, pad;
+  int retired[MAXSH];
 };
 
 struct FinMsAlpha {
@@ -1464,7 +1507,18 @@ struct FinMsUpdate {
     if (m.status == ST_RUN) {
       m.rsq = t[0];
       m.need_scroll = 1;
-      if ((m.rsqstop > 0 && m.rsq <= m.rsqstop) || m.iter >= m.niter || !isfinite(m.rsq)) m.status = ST_HOST;
+      if (m.rsqretire > 0)
+        for (int j = 0; j < m.num_now; j++)
+          if (j != m.j_low && m.zeta_ip1[j] * m.zeta_ip1[j] * m.rsq < m.rsqretire) m.retired[j] = 1;
+      if ((m.rsqstop > 0 && m.rsq <= m.rsqstop) || m.iter >= m.niter || !isfinite(m.rsq)) {
+        m.status = ST_HOST;
+      } else if (m.delta > 0) {
+        // sloppy solve: ask for a reliable update when |r| fell below
+        // delta * max|r| since the last one
+        double rn = sqrt(m.rsq);
+        if (rn > m.maxrr) m.maxrr = rn;
+        if (rn < m.delta * m.maxrr) { m.status = ST_HOST; m.want_reliable = 1; }
+      }
     }
     *skip = (m.status != ST_RUN);
   }
@@ -1494,6 +1548,7 @@ template <typename R> struct OpShiftUpdate {
       rr += rv.x * rv.x + rv.y * rv.y;
     }
     for (int j = 0; j < n; j++) {
+      if (m.retired[j]) continue;
       const R bj = (R)m.beta_i[j], zj = (R)m.zeta_ip1[j], aj = (R)m.alpha[j];
 #pragma unroll
       for (int k = 0; k < 3; k++) {
@@ -1562,24 +1617,69 @@ template <typename R> struct OpShiftInit {
   }
 };
 
-struct OpF32ToF64 {
-  const float2 *a[BLAS_MAXSRC];
-  double2 *b[BLAS_MAXSRC];
+// reliable update of the sloppy multi-shift solve, per shift:
+// x64_j += x32_j ; x32_j = 0
+struct OpMsFold {
+  double2 *x64[BLAS_MAXSRC];
+  float2 *x32[BLAS_MAXSRC];
   int Vh;
   __device__ void operator()(int h, int s, double *) const {
 #pragma unroll
     for (int k = 0; k < 3; k++) {
       size_t i = (size_t)k * Vh + h;
-      float2 v = a[s][i];
-      b[s][i] = make_double2(v.x, v.y);
+      double2 a = x64[s][i];
+      float2 b = x32[s][i];
+      x64[s][i] = make_double2(a.x + (double)b.x, a.y + (double)b.y);
+      x32[s][i] = make_float2(0.f, 0.f);
     }
   }
 };
 
-// sloppy (or FP64) multi-shift iterations; R selects vector storage precision
+// FP64 residual of the lowest shift, r = src - (sigma - D D) x with
+// ddx = D D x, stored into the sloppy r; |r|^2 in FP64
+struct OpMsResid {
+  const double2 *src, *ddx, *x;
+  float2 *r32;
+  double sigma;
+  int Vh;
+  __device__ void operator()(int h, int, double *out) const {
+    double a = 0;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      size_t i = (size_t)k * Vh + h;
+      double2 sv = src[i], dv = ddx[i], xv = x[i];
+      double2 rv = make_double2(sv.x + (dv.x - sigma * xv.x), sv.y + (dv.y - sigma * xv.y));
+      r32[i] = make_float2((float)rv.x, (float)rv.y);
+      a += rv.x * rv.x + rv.y * rv.y;
+    }
+    out[0] = a;
+  }
+};
+
+// x64_j += x32_j for every shift (FP32 sloppy solutions folded into FP64)
+static int ms_fold(int nsh, double2 *const *x64, void *const *x32) {
+  for (int b0 = 0; b0 < nsh; b0 += BLAS_MAXSRC) {
+    int nb = nsh - b0 < BLAS_MAXSRC ? nsh - b0 : BLAS_MAXSRC;
+    OpMsFold op;
+    memset(&op, 0, sizeof op);
+    for (int s = 0; s < nb; s++) { op.x64[s] = x64[b0 + s]; op.x32[s] = (float2 *)x32[b0 + s]; }
+    op.Vh = (int)ctx().Vh;
+    MKS_TRY((launch_site<OpMsFold, 0, FinNone>(MKS_K_SHIFT, op, FinNone(), nullptr, nb)));
+  }
+  return MKS_OK;
+}
+
+// sloppy (or FP64) multi-shift iterations; R selects vector storage precision.
+// With x64 given (sloppy storage only), the solve makes reliable updates:
+// when |r| fell below delta times its maximum since the last update, every
+// shift's FP32 solution is folded into its FP64 accumulator x64_j and the
+// residual of the lowest shift is recomputed in FP64 from x64_low and
+// replaces the sloppy one (the shifted residuals stay zeta_j r); on exit
+// x64_j holds the whole solution.
 template <typename R>
 static int multishift_core(const LinkSlot &sl, int par, int prec, const double2 *src64, int nsh,
-                           const double *offsets, double resid, int niter, void **psim_out, MsState *hstate) {
+                           const double *offsets, double resid, int niter, void **psim_out, MsState *hstate,
+                           double2 *const *x64 = nullptr, double delta = 0.0) {
   typedef typename VT<R>::v2 T2;
   Context &c = ctx();
   const int Vh = (int)c.Vh;
@@ -1635,7 +1735,14 @@ static int multishift_core(const LinkSlot &sl, int par, int prec, const double2 
     h.rsqstop = resid * resid * sn;
     h.iter = 1;
     h.status = sn == 0.0 ? ST_DONE : ST_RUN;
+    h.maxrr = sqrt(sn);
+    h.delta = (x64 && sizeof(R) == 4) ? delta : 0.0;
+    // sloppy solve: stop updating a shift once its iterated residual is a
+    // decade below the target (its true residual is checked afterwards)
+    h.rsqretire = h.delta > 0 ? 0.01 * h.rsqstop : 0.0;
   }
+  if (h.delta > 0)
+    for (int j = 0; j < nsh; j++) MKS_CUDA(cudaMemsetAsync(x64[j], 0, n * sizeof(double2), c.stream));
   MKS_CUDA(cudaMemcpyAsync(st, &h, sizeof h, cudaMemcpyHostToDevice, c.stream));
   int zero = 0;
   MKS_CUDA(cudaMemcpyAsync(skip, &zero, sizeof zero, cudaMemcpyHostToDevice, c.stream));
@@ -1693,7 +1800,30 @@ static int multishift_core(const LinkSlot &sl, int par, int prec, const double2 
     MKS_CUDA(cudaMemcpyAsync(&h, st, sizeof h, cudaMemcpyDeviceToHost, c.stream));
     MKS_CUDA(cudaStreamSynchronize(c.stream));
     if (++guard > 10000000) return MKS_ERR_TIMEOUT;
+    if (h.status == ST_HOST && h.want_reliable) {
+      // reliable update: fold, FP64 residual of the lowest shift, continue
+      MKS_TRY(ms_fold(nsh, x64, psim_out));
+      double2 *t64, *dd64;
+      MKS_TRY(wsv("ms_rel_t64", n, &t64));
+      MKS_TRY(wsv("ms_rel_dd64", n, &dd64));
+      double2 *xl = x64[h.j_low];
+      MKS_TRY(apply_DD64(sl, par, 1, &xl, &t64, &dd64));
+      OpMsResid op;
+      op.src = src64; op.ddx = dd64; op.x = xl; op.r32 = (float2 *)r; op.sigma = offsets[h.j_low]; op.Vh = Vh;
+      MKS_TRY((launch_site<OpMsResid, 1, FinNone>(MKS_K_SHIFT, op, FinNone(), nullptr, 1, tot)));
+      double rr = 0;
+      MKS_CUDA(cudaMemcpyAsync(&rr, tot, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+      MKS_CUDA(cudaStreamSynchronize(c.stream));
+      h.rsq = rr;
+      h.maxrr = sqrt(rr);
+      h.want_reliable = 0;
+      h.n_reliable++;
+      h.status = (h.rsq <= h.rsqstop || !std::isfinite(h.rsq)) ? ST_HOST : ST_RUN;
+      MKS_CUDA(cudaMemcpyAsync(st, &h, sizeof h, cudaMemcpyHostToDevice, c.stream));
+      MKS_CUDA(cudaMemcpyAsync(skip, &zero, sizeof zero, cudaMemcpyHostToDevice, c.stream));
+    }
   }
+  if (h.delta > 0) MKS_TRY(ms_fold(nsh, x64, psim_out));
   *hstate = h;
   return MKS_OK;
 }
@@ -1727,31 +1857,32 @@ static int multishift_dev(const double *src_dev, double *const *psim_dev, const 
     MKS_CUDA(cudaStreamSynchronize(c.stream));
     return h.iter;
   }
-  // sloppy multi-shift to at most 1e-5 (FP32 / FP16 vectors), then FP64-exact refinement of
-  // every shift by the mixed-precision CG (generic_ks/ks_multicg.c:170-228)
-  double sloppy_resid = arg->resid > 1e-5 ? arg->resid : 1e-5;
-  MKS_TRY(multishift_core<float>(sl, par, arg->prec, src64, nsh, offsets, sloppy_resid, niter, psim, &h));
+  // sloppy multi-shift (FP32 / FP16 vectors) with FP64 reliable updates of the
+  // lowest shift to the requested residual, the shifts' solutions accumulated
+  // in FP64; then each shift's true residual is checked in FP64 and the shifts
+  // that miss it are refined by the mixed-precision block CG
+  // (generic_ks/ks_multicg.c:170-228)
+  double2 *x64[MAXSH];
+  for (int j = 0; j < nsh; j++) MKS_TRY(wsv("ms_x64_" + std::to_string(j), 3 * c.Vh, &x64[j]));
+  MKS_TRY(multishift_core<float>(sl, par, arg->prec, src64, nsh, offsets, arg->resid, niter, psim, &h, x64,
+                                 arg->delta > 0 ? arg->delta : 0.1));
   int total_iters = h.iter;
   for (int b0 = 0; b0 < nsh; b0 += MAXSRC) {
     int nb = nsh - b0 < MAXSRC ? nsh - b0 : MAXSRC;
     CgFields f;
     memset(&f, 0, sizeof f);
     MKS_TRY(alloc_cg_fields(f, nb, arg->prec));
-    OpF32ToF64 cv;
-    memset(&cv, 0, sizeof cv);
     for (int s = 0; s < nb; s++) {
-      MKS_CUDA(cudaMemcpyAsync(f.src[s], src64, 3 * c.Vh * sizeof(double2), cudaMemcpyDeviceToDevice, c.stream));
-      cv.a[s] = (const float2 *)psim[b0 + s];
-      cv.b[s] = f.x[s];
+      f.src[s] = src64;       // read only in the block CG
+      f.x[s] = x64[b0 + s];   // the sloppy solve's FP64 solution is the initial guess
     }
-    cv.Vh = (int)c.Vh;
-    MKS_TRY((launch_site<OpF32ToF64, 0, FinNone>(MKS_K_BLAS, cv, FinNone(), nullptr, nb)));
     double sig[MAXSRC];
     for (int s = 0; s < nb; s++) sig[s] = offsets[b0 + s];
     MKS_TRY(block_cg_shifted(slot, par, nb, sig, arg, f, res + b0));
     for (int s = 0; s < nb; s++) {
       MKS_TRY(vec_soa64_to_aos(f.x[s], psim_dev[b0 + s], par));
       res[b0 + s].final_iters += total_iters;
+      res[b0 + s].reliable_updates += h.n_reliable;
     }
   }
   MKS_CUDA(cudaStreamSynchronize(c.stream));

@@ -1,30 +1,66 @@
-// mks_su3.cuh -- FP64 3x3 matrix helpers and link-field views shared by the
-// link-construction and fermion-force kernels.
+// mks_su3.cuh -- 3x3 matrix helpers and link-field views (FP64 or FP32
+// storage) shared by the link-construction and fermion-force kernels.
 #pragma once
 #include "mks_internal.cuh"
 
 namespace mks {
 
-// a 3x3 matrix per site: element k of site (par,h) at p[par*ps + k*Vh + h]
-struct MatF {
-  double2 *p;
+// storage element of a complex number in precision R
+template <typename R> struct Stor;
+template <> struct Stor<double> { typedef double2 t; };
+template <> struct Stor<float> { typedef float2 t; };
+
+// a 3x3 matrix per site stored in precision R: element k of site (par,h)
+// at p[par*ps + k*Vh + h]
+template <typename R>
+struct MatT {
+  typedef typename Stor<R>::t T2;
+  T2 *p;
   size_t ps;
-  __device__ __forceinline__ M3<double> ld(int par, int h, int Vh) const {
-    const double2 *b = p + par * ps + h;
-    M3<double> m;
+  __device__ __forceinline__ M3<R> ld(int par, int h, int Vh) const {
+    const T2 *b = p + par * ps + h;
+    M3<R> m;
 #pragma unroll
-    for (int k = 0; k < 9; k++) { double2 a = b[(size_t)k * Vh]; m.e[k / 3][k % 3] = {a.x, a.y}; }
+    for (int k = 0; k < 9; k++) { T2 a = b[(size_t)k * Vh]; m.e[k / 3][k % 3] = {a.x, a.y}; }
     return m;
   }
-  __device__ __forceinline__ void st(int par, int h, int Vh, const M3<double> &m) const {
-    double2 *b = p + par * ps + h;
+  __device__ __forceinline__ void st(int par, int h, int Vh, const M3<R> &m) const {
+    T2 *b = p + par * ps + h;
 #pragma unroll
-    for (int k = 0; k < 9; k++) b[(size_t)k * Vh] = make_double2(m.e[k / 3][k % 3].re, m.e[k / 3][k % 3].im);
+    for (int k = 0; k < 9; k++) b[(size_t)k * Vh] = {m.e[k / 3][k % 3].re, m.e[k / 3][k % 3].im};
   }
 };
+typedef MatT<double> MatF;
 
-__host__ __device__ inline MatF link_dir(double2 *base, int dir, size_t Vh) { return {base + (size_t)dir * 9 * Vh, 36 * Vh}; }
-__host__ __device__ inline MatF mat_field(double2 *base, size_t Vh) { return {base, 9 * Vh}; }
+// views of a link field [par][dir][9][Vh] (one direction) and of a single
+// matrix field [par][9][Vh]
+__host__ __device__ inline MatT<double> link_dir(double2 *base, int dir, size_t Vh) {
+  return {base + (size_t)dir * 9 * Vh, 36 * Vh};
+}
+__host__ __device__ inline MatT<float> link_dir(float2 *base, int dir, size_t Vh) {
+  return {base + (size_t)dir * 9 * Vh, 36 * Vh};
+}
+__host__ __device__ inline MatT<double> mat_field(double2 *base, size_t Vh) { return {base, 9 * Vh}; }
+__host__ __device__ inline MatT<float> mat_field(float2 *base, size_t Vh) { return {base, 9 * Vh}; }
+
+// y = a x + b y, and precision conversions, over n complex numbers
+template <typename T2>
+__global__ void k_axpby_t(const T2 *x, T2 *y, double a, double b, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    typedef decltype(T2::x) E;
+    const E ae = (E)a, be = (E)b;
+    T2 u = x[i], v = y[i];
+    y[i] = {ae * u.x + be * v.x, ae * u.y + be * v.y};
+  }
+}
+template <typename TO, typename TI>
+__global__ void k_convert(const TI *x, TO *y, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    typedef decltype(TO::x) E;
+    TI u = x[i];
+    y[i] = {(E)u.x, (E)u.y};
+  }
+}
 
 __device__ __forceinline__ M3<double> mm_nn(const M3<double> &a, const M3<double> &b) {
   M3<double> c;
@@ -75,26 +111,7 @@ __device__ __forceinline__ M3<double> mm_an(const M3<double> &a, const M3<double
   return c;
 }
 
-// the same products in arithmetic R (FP64 fields converted on load and back
-// on store: FP32 arithmetic runs at many times the FP64 rate on GB300)
-template <typename R>
-__device__ __forceinline__ M3<R> narrow(const M3<double> &m) {
-  M3<R> o;
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) o.e[i][j] = {(R)m.e[i][j].re, (R)m.e[i][j].im};
-  return o;
-}
-template <typename R>
-__device__ __forceinline__ M3<double> widen(const M3<R> &m) {
-  M3<double> o;
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) o.e[i][j] = {(double)m.e[i][j].re, (double)m.e[i][j].im};
-  return o;
-}
+// the same products in arithmetic R
 template <typename R>
 __device__ __forceinline__ M3<R> tnn(const M3<R> &a, const M3<R> &b) {
   M3<R> c;
@@ -182,11 +199,11 @@ __device__ __forceinline__ int nbr2(const Geom &g, int par, int h, int mu, int d
 
 // generalised staple S(x) = U_nu(x) A(x+nu) U_nu(x+mu)^dag + U_nu(x-nu)^dag A(x-nu) U_nu(x-nu+mu)
 // (generic/general_staple.c:42-140): S saved when sout.p != nullptr, and
-// fat_mu(x) += coef * S(x) when fat.p != nullptr; products in arithmetic R,
-// fields and the accumulation FP64
+// fat_mu(x) += coef * S(x) when fat.p != nullptr; fields stored and
+// products computed in precision R
 template <typename R>
-static __global__ void __launch_bounds__(128) k_staple(Geom g, int mu, int nu, MatF Unu, MatF A, MatF fat, double coef,
-                                                       MatF sout) {
+static __global__ void __launch_bounds__(128) k_staple(Geom g, int mu, int nu, MatT<R> Unu, MatT<R> A, MatT<R> fat,
+                                                       double coef, MatT<R> sout) {
   const int h = blockIdx.x * blockDim.x + threadIdx.x;
   const int par = blockIdx.y, opar = 1 - par;
   const int Vh = g.Vh;
@@ -194,26 +211,24 @@ static __global__ void __launch_bounds__(128) k_staple(Geom g, int mu, int nu, M
   const int xpnu = nbr(g, par, h, nu, 1), xpmu = nbr(g, par, h, mu, 1), xmnu = nbr(g, par, h, nu, -1);
   const int xmnupmu = nbr2(g, par, h, nu, -1, mu, 1);
   // upper: U_nu(x) [A(x+nu) U_nu(x+mu)^dag]
-  M3<R> up = tnn<R>(narrow<R>(Unu.ld(par, h, Vh)),
-                    tna<R>(narrow<R>(A.ld(opar, xpnu, Vh)), narrow<R>(Unu.ld(opar, xpmu, Vh))));
+  M3<R> up = tnn<R>(Unu.ld(par, h, Vh), tna<R>(A.ld(opar, xpnu, Vh), Unu.ld(opar, xpmu, Vh)));
   // lower: [U_nu(x-nu)^dag A(x-nu)] U_nu(x-nu+mu)
-  M3<R> dn = tnn<R>(tan_<R>(narrow<R>(Unu.ld(opar, xmnu, Vh)), narrow<R>(A.ld(opar, xmnu, Vh))),
-                    narrow<R>(Unu.ld(par, xmnupmu, Vh)));
-  M3<double> s;
+  M3<R> dn = tnn<R>(tan_<R>(Unu.ld(opar, xmnu, Vh), A.ld(opar, xmnu, Vh)), Unu.ld(par, xmnupmu, Vh));
+  M3<R> s;
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
-    for (int j = 0; j < 3; j++)
-      s.e[i][j] = {(double)up.e[i][j].re + (double)dn.e[i][j].re, (double)up.e[i][j].im + (double)dn.e[i][j].im};
+    for (int j = 0; j < 3; j++) s.e[i][j] = {up.e[i][j].re + dn.e[i][j].re, up.e[i][j].im + dn.e[i][j].im};
   if (sout.p) sout.st(par, h, Vh, s);
   if (!fat.p) return;
-  M3<double> f = fat.ld(par, h, Vh);
+  M3<R> f = fat.ld(par, h, Vh);
+  const R c = (R)coef;
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = 0; j < 3; j++) {
-      f.e[i][j].re += coef * s.e[i][j].re;
-      f.e[i][j].im += coef * s.e[i][j].im;
+      f.e[i][j].re += c * s.e[i][j].re;
+      f.e[i][j].im += c * s.e[i][j].im;
     }
   fat.st(par, h, Vh, f);
 }
