@@ -73,6 +73,26 @@ struct NoFinish {
 #define MKS_DSLASH_BOUNDS(NB) __launch_bounds__(256)
 #endif
 
+// checkerboard indices of the +-1 and +-3 neighbours along mu of the site with coordinates c0
+__device__ __forceinline__ void nbr4(const Geom &g, const int c0[4], const int L[4], int mu, int &hf1, int &hb1,
+                                     int &hf3, int &hb3) {
+  int cf1[4] = {c0[0], c0[1], c0[2], c0[3]}, cb1[4] = {c0[0], c0[1], c0[2], c0[3]};
+  int cf3[4] = {c0[0], c0[1], c0[2], c0[3]}, cb3[4] = {c0[0], c0[1], c0[2], c0[3]};
+  cf1[mu] = wrap_add(c0[mu], 1, L[mu]);
+  cb1[mu] = wrap_add(c0[mu], -1, L[mu]);
+  cf3[mu] = wrap_add(c0[mu], 3, L[mu]);
+  cb3[mu] = wrap_add(c0[mu], -3, L[mu]);
+  hf1 = cb_index(g, cf1[0], cf1[1], cf1[2], cf1[3]);
+  hb1 = cb_index(g, cb1[0], cb1[1], cb1[2], cb1[3]);
+  hf3 = cb_index(g, cf3[0], cf3[1], cf3[2], cf3[3]);
+  hb3 = cb_index(g, cb3[0], cb3[1], cb3[2], cb3[3]);
+}
+
+// prefetch of the next direction's operands into L2 (see k_dslash)
+#ifndef MKS_NBR_PREFETCH
+#define MKS_NBR_PREFETCH 0
+#endif
+
 template <typename R, class LinkT, class InT, class OutT, int NB, int EPI, int NSUM, class Fin>
 __global__ void MKS_DSLASH_BOUNDS(NB)
 k_dslash(const LinkT fat, const LinkT lng, const DslashArgs<InT, OutT, typename EpiLoad<R>::type> a,
@@ -118,16 +138,31 @@ k_dslash(const LinkT fat, const LinkT lng, const DslashArgs<InT, OutT, typename 
     const int L[4] = {g.nx, g.ny, g.nz, g.nt};
 #pragma unroll
     for (int mu = 0; mu < 4; mu++) {
-      int cf1[4] = {c0[0], c0[1], c0[2], c0[3]}, cb1[4] = {c0[0], c0[1], c0[2], c0[3]};
-      int cf3[4] = {c0[0], c0[1], c0[2], c0[3]}, cb3[4] = {c0[0], c0[1], c0[2], c0[3]};
-      cf1[mu] = wrap_add(c0[mu], 1, L[mu]);
-      cb1[mu] = wrap_add(c0[mu], -1, L[mu]);
-      cf3[mu] = wrap_add(c0[mu], 3, L[mu]);
-      cb3[mu] = wrap_add(c0[mu], -3, L[mu]);
-      const int hf1 = cb_index(g, cf1[0], cf1[1], cf1[2], cf1[3]);
-      const int hb1 = cb_index(g, cb1[0], cb1[1], cb1[2], cb1[3]);
-      const int hf3 = cb_index(g, cf3[0], cf3[1], cf3[2], cf3[3]);
-      const int hb3 = cb_index(g, cb3[0], cb3[1], cb3[2], cb3[3]);
+      int hf1, hb1, hf3, hb3;
+      nbr4(g, c0, L, mu, hf1, hb1, hf3, hb3);
+      if (MKS_NBR_PREFETCH && mu < 3) {
+        // bring the next direction's links and neighbour vectors into L2
+        // while this direction computes: the thread whose index starts a
+        // 128-byte line fetches that line
+        int pf1, pb1, pf3, pb3;
+        nbr4(g, c0, L, mu + 1, pf1, pb1, pf3, pb3);
+#pragma unroll
+        for (int s = 0; s < NB; s++) {
+          const int S = grp * NB + s;
+          if (S < a.nsrc) {
+            a.in[S].prefetch_line(pf1, Vh);
+            a.in[S].prefetch_line(pb1, Vh);
+            a.in[S].prefetch_line(pf3, Vh);
+            a.in[S].prefetch_line(pb3, Vh);
+          }
+        }
+        if (grp == 0) {
+          fat.prefetch_line(par, mu + 1, h, Vh);
+          lng.prefetch_line(par, mu + 1, h, Vh);
+          fat.prefetch_line(opar, mu + 1, pb1, Vh);
+          lng.prefetch_line(opar, mu + 1, pb3, Vh);
+        }
+      }
       {
         const M3<R> U = load_link(fat, par, mu, h, Vh);
 #pragma unroll
