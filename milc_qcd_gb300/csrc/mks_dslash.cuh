@@ -63,14 +63,11 @@ struct NoFinish {
 };
 
 // minimum resident 256-thread blocks per SM asked of the register allocator
-// for the kernels with up to 4 sources per thread (0: no request)
-#ifndef MKS_DSLASH_MINB
-#define MKS_DSLASH_MINB 0
-#endif
-#if MKS_DSLASH_MINB > 0
-#define MKS_DSLASH_BOUNDS(NB) __launch_bounds__(256, (NB) <= 4 ? MKS_DSLASH_MINB : 1)
-#else
-#define MKS_DSLASH_BOUNDS(NB) __launch_bounds__(256)
+// for the single-source kernel (one thread per site, one source): measured on
+// GB300, 4 gives the FP32 single-source CG 6-8 % more D_eo throughput; asking
+// it of the multi-source shapes slows them (register spills)
+#ifndef MKS_DSLASH1_MINB
+#define MKS_DSLASH1_MINB 4
 #endif
 
 // checkerboard indices of the +-1 and +-3 neighbours along mu of the site with coordinates c0
@@ -88,15 +85,10 @@ __device__ __forceinline__ void nbr4(const Geom &g, const int c0[4], const int L
   hb3 = cb_index(g, cb3[0], cb3[1], cb3[2], cb3[3]);
 }
 
-// prefetch of the next direction's operands into L2 (see k_dslash)
-#ifndef MKS_NBR_PREFETCH
-#define MKS_NBR_PREFETCH 0
-#endif
-
 template <typename R, class LinkT, class InT, class OutT, int NB, int EPI, int NSUM, class Fin>
-__global__ void MKS_DSLASH_BOUNDS(NB)
-k_dslash(const LinkT fat, const LinkT lng, const DslashArgs<InT, OutT, typename EpiLoad<R>::type> a,
-         const Fin fin) {
+__device__ __forceinline__ void dslash_body(const LinkT &fat, const LinkT &lng,
+                                            const DslashArgs<InT, OutT, typename EpiLoad<R>::type> &a,
+                                            const Fin &fin) {
   typedef typename EpiLoad<R>::type EpiT;
   if (a.skip && *a.skip) return;
   const Geom &g = a.g;
@@ -140,29 +132,6 @@ k_dslash(const LinkT fat, const LinkT lng, const DslashArgs<InT, OutT, typename 
     for (int mu = 0; mu < 4; mu++) {
       int hf1, hb1, hf3, hb3;
       nbr4(g, c0, L, mu, hf1, hb1, hf3, hb3);
-      if (MKS_NBR_PREFETCH && mu < 3) {
-        // bring the next direction's links and neighbour vectors into L2
-        // while this direction computes: the thread whose index starts a
-        // 128-byte line fetches that line
-        int pf1, pb1, pf3, pb3;
-        nbr4(g, c0, L, mu + 1, pf1, pb1, pf3, pb3);
-#pragma unroll
-        for (int s = 0; s < NB; s++) {
-          const int S = grp * NB + s;
-          if (S < a.nsrc) {
-            a.in[S].prefetch_line(pf1, Vh);
-            a.in[S].prefetch_line(pb1, Vh);
-            a.in[S].prefetch_line(pf3, Vh);
-            a.in[S].prefetch_line(pb3, Vh);
-          }
-        }
-        if (grp == 0) {
-          fat.prefetch_line(par, mu + 1, h, Vh);
-          lng.prefetch_line(par, mu + 1, h, Vh);
-          fat.prefetch_line(opar, mu + 1, pb1, Vh);
-          lng.prefetch_line(opar, mu + 1, pb3, Vh);
-        }
-      }
       {
         const M3<R> U = load_link(fat, par, mu, h, Vh);
 #pragma unroll
@@ -244,6 +213,22 @@ k_dslash(const LinkT fat, const LinkT lng, const DslashArgs<InT, OutT, typename 
       fin(tot, a.nsrc);
     }
   }
+}
+
+// the multi-source shapes (G threads per site x NB sources per thread)
+template <typename R, class LinkT, class InT, class OutT, int NB, int EPI, int NSUM, class Fin>
+__global__ void __launch_bounds__(256)
+k_dslash(const LinkT fat, const LinkT lng, const DslashArgs<InT, OutT, typename EpiLoad<R>::type> a,
+         const Fin fin) {
+  dslash_body<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin>(fat, lng, a, fin);
+}
+
+// one source, one thread per site (G = NB = 1)
+template <typename R, class LinkT, class InT, class OutT, int EPI, int NSUM, class Fin>
+__global__ void __launch_bounds__(256, MKS_DSLASH1_MINB)
+k_dslash1(const LinkT fat, const LinkT lng, const DslashArgs<InT, OutT, typename EpiLoad<R>::type> a,
+          const Fin fin) {
+  dslash_body<R, LinkT, InT, OutT, 1, EPI, NSUM, Fin>(fat, lng, a, fin);
 }
 
 }  // namespace mks

@@ -137,12 +137,6 @@ struct VecF64 {
       if (h + 8 < Vh) prefetch_l2(p + (size_t)c * Vh + h + 8);
     }
   }
-  // the 128-byte lines that start at site h (a no-op unless h starts a line)
-  __device__ __forceinline__ void prefetch_line(int h, int Vh) const {
-    if (h & 7) return;
-#pragma unroll
-    for (int c = 0; c < 3; c++) prefetch_l2(p + (size_t)c * Vh + h);
-  }
   __device__ __forceinline__ V3<double> load(int h, int Vh) const {
     V3<double> v;
 #pragma unroll
@@ -158,11 +152,6 @@ struct VecF32 {
   float2 *p;  // [3][Vh]
   // lines of the 16 sites h..h+15 (h a multiple of 16)
   __device__ __forceinline__ void prefetch16(int h, int Vh) const {
-#pragma unroll
-    for (int c = 0; c < 3; c++) prefetch_l2(p + (size_t)c * Vh + h);
-  }
-  __device__ __forceinline__ void prefetch_line(int h, int Vh) const {
-    if (h & 15) return;
 #pragma unroll
     for (int c = 0; c < 3; c++) prefetch_l2(p + (size_t)c * Vh + h);
   }
@@ -186,12 +175,6 @@ struct VecF32 {
 struct VecF16 {
   __half2 *p;   // [3][Vh]
   float *norm;  // [Vh]
-  __device__ __forceinline__ void prefetch_line(int h, int Vh) const {
-    if (h & 31) return;
-#pragma unroll
-    for (int c = 0; c < 3; c++) prefetch_l2(p + (size_t)c * Vh + h);
-    prefetch_l2(norm + h);
-  }
   __device__ __forceinline__ V3<float> load(int h, int Vh) const {
     V3<float> v;
     float s = __ldg(norm + h);
@@ -226,12 +209,6 @@ struct VecF16 {
 struct LinkF64 {
   static constexpr bool scaled = false;
   const double2 *p;  // [par][dir][9][Vh]
-  __device__ __forceinline__ void prefetch_line(int par, int dir, int h, int Vh) const {
-    if (h & 7) return;
-    const double2 *b = p + ((size_t)(par * 4 + dir) * 9) * Vh + h;
-#pragma unroll
-    for (int k = 0; k < 9; k++) prefetch_l2(b + (size_t)k * Vh);
-  }
   __device__ __forceinline__ M3<double> load(int par, int dir, int h, int Vh) const {
     const double2 *b = p + ((size_t)(par * 4 + dir) * 9) * Vh + h;
     M3<double> m;
@@ -244,13 +221,6 @@ struct LinkF32 {
   static constexpr bool scaled = false;
   const float4 *a;  // [par][dir][4][Vh]
   const float2 *b;  // [par][dir][Vh]
-  __device__ __forceinline__ void prefetch_line(int par, int dir, int h, int Vh) const {
-    if (h & 7) return;
-    const float4 *pa = a + ((size_t)(par * 4 + dir) * 4) * Vh + h;
-#pragma unroll
-    for (int k = 0; k < 4; k++) prefetch_l2(pa + (size_t)k * Vh);
-    if (!(h & 15)) prefetch_l2(b + (size_t)(par * 4 + dir) * Vh + h);
-  }
   __device__ __forceinline__ M3<float> load(int par, int dir, int h, int Vh) const {
     const float4 *pa = a + ((size_t)(par * 4 + dir) * 4) * Vh + h;
     float2 l = __ldg(b + (size_t)(par * 4 + dir) * Vh + h);
@@ -270,13 +240,6 @@ struct LinkF16 {
   const uint4 *a;     // [par][dir][2][Vh]: entries 0..7 as 16 halves
   const __half2 *b;   // [par][dir][Vh]: entry 8
   float scale;
-  __device__ __forceinline__ void prefetch_line(int par, int dir, int h, int Vh) const {
-    if (h & 7) return;
-    const uint4 *pa = a + ((size_t)(par * 4 + dir) * 2) * Vh + h;
-    prefetch_l2(pa);
-    prefetch_l2(pa + Vh);
-    if (!(h & 31)) prefetch_l2(b + (size_t)(par * 4 + dir) * Vh + h);
-  }
   // unscaled entries: U = scale * load_raw(); D_eo folds `scale` into the vector
   __device__ __forceinline__ M3<float> load_raw(int par, int dir, int h, int Vh) const {
     const uint4 *pa = a + ((size_t)(par * 4 + dir) * 2) * Vh + h;

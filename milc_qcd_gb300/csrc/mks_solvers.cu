@@ -380,7 +380,10 @@ static int launch_dslash_nb(int family, const LinkT &fat, const LinkT &lng,
     a.red = c.red;
   }
   timing_begin(family);
-  k_dslash<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin><<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
+  if (NB == 1 && a.groups == 1 && block == 256)
+    k_dslash1<R, LinkT, InT, OutT, EPI, NSUM, Fin><<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
+  else
+    k_dslash<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin><<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
   timing_end(family);
   MKS_CUDA(cudaGetLastError());
   return MKS_OK;
