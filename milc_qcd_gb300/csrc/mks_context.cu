@@ -146,7 +146,10 @@ int red_check() {
   MKS_CUDA(cudaStreamSynchronize(c.stream));
   if (!e) return MKS_OK;
   MKS_CUDA(cudaMemsetAsync(c.red.err, 0, sizeof(int), c.stream));
-  snprintf(g_errmsg, sizeof g_errmsg, "reduction scratch too small for a launch (internal sizing error)");
+  if (e & 2)
+    snprintf(g_errmsg, sizeof g_errmsg, "D_eo link staging did not complete within its wait limit");
+  else
+    snprintf(g_errmsg, sizeof g_errmsg, "reduction scratch too small for a launch (internal sizing error)");
   return MKS_ERR_CUDA;
 }
 

@@ -85,10 +85,39 @@ __device__ __forceinline__ void nbr4(const Geom &g, const int c0[4], const int L
   hb3 = cb_index(g, cb3[0], cb3[1], cb3[2], cb3[3]);
 }
 
-template <typename R, class LinkT, class InT, class OutT, int NB, int EPI, int NSUM, class Fin>
+// ---- links of a tile staged in shared memory by the TMA engine ----
+// A tile is T = R x nx/2 consecutive output sites: R complete x-rows of one
+// (z, t) plane.  Its 16 links per site (fat / Naik, forward at the site,
+// backward at the -1 / -3 neighbour) are copied by cp.async.bulk into
+// shared memory, link l = 4 mu + kind (kind 0 fat forward, 1 Naik forward,
+// 2 fat backward, 3 Naik backward) at byte offset 72 T l: the four float4
+// planes of FP32 entries 0..7 (T x 16 B each) and the float2 plane of
+// entry 8 (T x 8 B).  The backward links along y, z, t are the rows of the
+// shifted rows or planes, copied in row order (at most two segments where
+// y wraps), so site i of the tile finds its backward link at slot i; along
+// x they are the tile's own rows of the other parity, slot hb - h0.
+struct TileSmem {
+  const unsigned char *base;
+  int T;
+  __device__ __forceinline__ M3<float> link(int l, int j) const {
+    const unsigned char *r = base + (size_t)l * 72 * T;
+    M3<float> m;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const float4 q = *reinterpret_cast<const float4 *>(r + (size_t)k * 16 * T + 16 * j);
+      m.e[(2 * k) / 3][(2 * k) % 3] = {q.x, q.y};
+      m.e[(2 * k + 1) / 3][(2 * k + 1) % 3] = {q.z, q.w};
+    }
+    const float2 e = *reinterpret_cast<const float2 *>(r + (size_t)64 * T + 8 * j);
+    m.e[2][2] = {e.x, e.y};
+    return m;
+  }
+};
+
+template <typename R, class LinkT, class InT, class OutT, int NB, int EPI, int NSUM, class Fin, bool TMA = false>
 __device__ __forceinline__ void dslash_body(const LinkT &fat, const LinkT &lng,
                                             const DslashArgs<InT, OutT, typename EpiLoad<R>::type> &a,
-                                            const Fin &fin) {
+                                            const Fin &fin, const TileSmem ts = TileSmem{nullptr, 0}) {
   typedef typename EpiLoad<R>::type EpiT;
   if (a.skip && *a.skip) return;
   const Geom &g = a.g;
@@ -132,8 +161,14 @@ __device__ __forceinline__ void dslash_body(const LinkT &fat, const LinkT &lng,
     for (int mu = 0; mu < 4; mu++) {
       int hf1, hb1, hf3, hb3;
       nbr4(g, c0, L, mu, hf1, hb1, hf3, hb3);
+      // tile-local slots of the staged links (TMA): the site's own slot, or
+      // along x the slot of the backward neighbour within the tile's rows
+      const int i0 = TMA ? h - (int)(blockIdx.x * ts.T) : 0;
+      const int jb1 = (TMA && mu == 0) ? hb1 - (h - i0) : i0, jb3 = (TMA && mu == 0) ? hb3 - (h - i0) : i0;
       {
-        const M3<R> U = load_link(fat, par, mu, h, Vh);
+        M3<R> U;
+        if constexpr (TMA) U = ts.link(4 * mu + 0, i0);
+        else U = load_link(fat, par, mu, h, Vh);
 #pragma unroll
         for (int s = 0; s < NB; s++) {
           const int S = grp * NB + s;
@@ -141,7 +176,9 @@ __device__ __forceinline__ void dslash_body(const LinkT &fat, const LinkT &lng,
         }
       }
       {
-        const M3<R> U = load_link(lng, par, mu, h, Vh);
+        M3<R> U;
+        if constexpr (TMA) U = ts.link(4 * mu + 1, i0);
+        else U = load_link(lng, par, mu, h, Vh);
 #pragma unroll
         for (int s = 0; s < NB; s++) {
           const int S = grp * NB + s;
@@ -149,7 +186,9 @@ __device__ __forceinline__ void dslash_body(const LinkT &fat, const LinkT &lng,
         }
       }
       {
-        const M3<R> U = load_link(fat, opar, mu, hb1, Vh);
+        M3<R> U;
+        if constexpr (TMA) U = ts.link(4 * mu + 2, jb1);
+        else U = load_link(fat, opar, mu, hb1, Vh);
 #pragma unroll
         for (int s = 0; s < NB; s++) {
           const int S = grp * NB + s;
@@ -157,7 +196,9 @@ __device__ __forceinline__ void dslash_body(const LinkT &fat, const LinkT &lng,
         }
       }
       {
-        const M3<R> U = load_link(lng, opar, mu, hb3, Vh);
+        M3<R> U;
+        if constexpr (TMA) U = ts.link(4 * mu + 3, jb3);
+        else U = load_link(lng, opar, mu, hb3, Vh);
 #pragma unroll
         for (int s = 0; s < NB; s++) {
           const int S = grp * NB + s;
@@ -229,6 +270,119 @@ __global__ void __launch_bounds__(256, MKS_DSLASH1_MINB)
 k_dslash1(const LinkT fat, const LinkT lng, const DslashArgs<InT, OutT, typename EpiLoad<R>::type> a,
           const Fin fin) {
   dslash_body<R, LinkT, InT, OutT, 1, EPI, NSUM, Fin>(fat, lng, a, fin);
+}
+
+// ---- TMA (cp.async.bulk) helpers ----
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t phase) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait: false when the phase did not complete within `limit` polls
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t phase, int limit) {
+  for (int it = 0; it < limit; it++)
+    if (mbar_try_wait(bar, phase)) return true;
+  return false;
+}
+// global -> shared bulk copy (16-byte aligned addresses, size a multiple of 16)
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// the (up to two) contiguous source segments of link l = 4 mu + kind for the
+// tile that starts at h0: seg 0 / 1 -> (first source site, first slot, sites);
+// false when the segment does not exist
+__device__ __forceinline__ bool tile_segment(const Geom &g, int T, int R, int h0, int l, int seg, int &src0,
+                                             int &loc0, int &cnt) {
+  const int mu = l >> 2, kind = l & 3;
+  const int s = kind < 2 ? 0 : (kind == 2 ? 1 : 3);
+  const int nx2 = g.nx >> 1;
+  const int row = h0 / nx2, y0 = row % g.ny, pz = row / g.ny, z = pz % g.nz, t = pz / g.nz;
+  if (s == 0 || mu == 0) {
+    if (seg) return false;
+    src0 = h0; loc0 = 0; cnt = T;
+    return true;
+  }
+  if (mu == 1) {
+    int yr = y0 - s;
+    if (yr < 0) yr += g.ny;
+    const int n1 = min(R, g.ny - yr);
+    const int pbase = pz * g.ny * nx2;
+    if (seg == 0) { src0 = pbase + yr * nx2; loc0 = 0; cnt = n1 * nx2; return true; }
+    if (n1 == R) return false;
+    src0 = pbase; loc0 = n1 * nx2; cnt = (R - n1) * nx2;
+    return true;
+  }
+  if (seg) return false;
+  if (mu == 2) {
+    int zz = z - s;
+    if (zz < 0) zz += g.nz;
+    src0 = ((t * g.nz + zz) * g.ny + y0) * nx2;
+  } else {
+    int tt = t - s;
+    if (tt < 0) tt += g.nt;
+    src0 = ((tt * g.nz + z) * g.ny + y0) * nx2;
+  }
+  loc0 = 0; cnt = T;
+  return true;
+}
+
+// FP32 multi-source D_eo with the links of each tile of T sites staged in
+// shared memory by the TMA engine (one thread per site and source, G
+// threads per site; blockDim = T G).  Warp 0 issues the bulk copies, every
+// thread waits on the tile's mbarrier with a bounded poll; a wait that runs
+// out sets bit 2 of the reduction error flag (read by the host at each poll)
+// and the kernel still returns.
+template <int EPI, int NSUM, class Fin>
+__global__ void __launch_bounds__(256)
+k_dslash_tma(const LinkF32 fat, const LinkF32 lng, const DslashArgs<VecF32, VecF32, VecF32> a, const Fin fin,
+             int T, int R) {
+  extern __shared__ __align__(128) unsigned char tsm[];
+  __shared__ __align__(8) uint64_t bar;
+  if (a.skip && *a.skip) return;
+  const Geom &g = a.g;
+  const int Vh = g.Vh, par = a.out_par, opar = 1 - par;
+  const int h0 = blockIdx.x * T;
+  if (threadIdx.x == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    if (threadIdx.x == 0) mbar_expect_tx(&bar, (uint32_t)T * 1152u);
+    __syncwarp();
+    for (int c = threadIdx.x; c < 160; c += 32) {
+      const int l = c / 10, q = (c % 10) >> 1, seg = c & 1;
+      int src0, loc0, cnt;
+      if (!tile_segment(g, T, R, h0, l, seg, src0, loc0, cnt)) continue;
+      const int mu = l >> 2, kind = l & 3;
+      const LinkF32 &L = (kind & 1) ? lng : fat;
+      const int sp = kind < 2 ? par : opar;
+      unsigned char *reg = tsm + (size_t)l * 72 * T;
+      if (q < 4)
+        bulk_g2s(reg + (size_t)q * 16 * T + 16 * loc0, L.a + ((size_t)(sp * 4 + mu) * 4 + q) * Vh + src0,
+                 (uint32_t)cnt * 16u, &bar);
+      else
+        bulk_g2s(reg + (size_t)64 * T + 8 * loc0, L.b + (size_t)(sp * 4 + mu) * Vh + src0, (uint32_t)cnt * 8u, &bar);
+    }
+  }
+  if (!mbar_wait_bounded(&bar, 0, 1 << 22)) {
+    if (a.red.err) atomicOr(a.red.err, 2);
+    mbar_wait_bounded(&bar, 0, 1 << 22);  // let copies in flight land before the block exits
+  }
+  dslash_body<float, LinkF32, VecF32, VecF32, 1, EPI, NSUM, Fin, true>(fat, lng, a, fin, TileSmem{tsm, T});
 }
 
 }  // namespace mks

@@ -17,6 +17,7 @@
 #include <cstdlib>
 #include <map>
 #include <string>
+#include <type_traits>
 #include <vector>
 #include "mks_internal.cuh"
 #include "mks_dslash.cuh"
@@ -43,9 +44,12 @@ static int ws(const std::string &name, size_t bytes, void **out) {
 }
 
 void graphs_free_all();
+static void shapes_reset();
 
+// on a lattice change: graphs, workspace and the tuned launch shapes go
 void ws_free_all() {
   graphs_free_all();
+  shapes_reset();
   for (auto &kv : g_ws) dev_free(kv.second.p);
   g_ws.clear();
 }
@@ -352,16 +356,42 @@ static LinkSet16 links16(const LinkSlot &s) {
 // vectors, keeps the fastest, and reuses it for every epilogue.  MKS_TUNE=0
 // turns tuning off (fixed table); the choices can be read back with
 // mks_tuned_shape().
-struct Shape { int G, NB, block; };
+// launch shape: G threads per site, NB sources per thread, block size;
+// tma = 1: the FP32 kernel that stages each tile's links in shared memory
+// (NB = 1, block = T G for a tile of T sites)
+struct Shape { int G, NB, block, tma; };
 static Shape g_shape[3][MAXSRC + 1];      // [prec][nsrc], G == 0: not chosen yet
 static Shape g_shape_epi[3][MAXSRC + 1];  // the same for the fused-epilogue launches
+static void shapes_reset() {
+  memset(g_shape, 0, sizeof g_shape);
+  memset(g_shape_epi, 0, sizeof g_shape_epi);
+}
 
 static Shape default_shape(int nsrc) {
-  if (nsrc <= 1) return {1, 1, 256};
-  if (nsrc <= 2) return {1, 2, 256};
-  if (nsrc <= 4) return {1, 4, 256};
-  if (nsrc <= 8) return {2, 4, 256};
-  return {4, 4, 256};
+  if (nsrc <= 1) return {1, 1, 256, 0};
+  if (nsrc <= 2) return {1, 2, 256, 0};
+  if (nsrc <= 4) return {1, 4, 256, 0};
+  if (nsrc <= 8) return {2, 4, 256, 0};
+  return {4, 4, 256, 0};
+}
+
+// tile of the TMA kernel for G threads per site: R complete x-rows of nx/2
+// sites (R dividing ny), T G <= 256 threads, a whole number of warps; the
+// bulk copies need nx/2 even (16-byte aligned row segments).  false when
+// the lattice admits no such tile.
+constexpr int TMA_MAX_SMEM = 200 * 1024;  // dynamic shared memory of the staged links, bytes
+static bool tma_tile(const Geom &g, int G, int *T, int *R) {
+  if (g.nx % 4 || g.ny < 4 || g.nz < 4 || g.nt < 4 || G < 1 || G > 16) return false;
+  const int nx2 = g.nx / 2;
+  for (int r = g.ny; r >= 1; r--) {
+    if (g.ny % r) continue;
+    const int t = r * nx2;
+    if (t * G > 256 || (t * G) % 32 || (size_t)t * 1152 > (size_t)TMA_MAX_SMEM) continue;
+    *T = t;
+    *R = r;
+    return true;
+  }
+  return false;
 }
 
 template <class LinkT> struct PrecOf;
@@ -394,6 +424,29 @@ static int launch_shape(int family, const LinkT &fat, const LinkT &lng,
                         DslashArgs<InT, OutT, typename EpiLoad<R>::type> &a, const Fin &fin, const Shape &sh) {
   a.groups = sh.G;
   a.g = ctx().geom;
+  if constexpr (std::is_same<LinkT, LinkF32>::value && std::is_same<InT, VecF32>::value &&
+                std::is_same<OutT, VecF32>::value) {
+    if (sh.tma) {
+      Context &c = ctx();
+      int T, Rr;
+      if (sh.NB != 1 || !tma_tile(a.g, sh.G, &T, &Rr) || a.nsrc > sh.G) return MKS_ERR_ARG;
+      const int grid = (int)(c.Vh / T);
+      const size_t smem = (size_t)T * 1152;
+      static bool attr = false;
+      if (!attr) {
+        MKS_CUDA(cudaFuncSetAttribute(k_dslash_tma<EPI, NSUM, Fin>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      TMA_MAX_SMEM));
+        attr = true;
+      }
+      MKS_TRY(ensure_red(NSUM > 0 ? NSUM * sh.G : 1, grid));
+      a.red = c.red;
+      timing_begin(family);
+      k_dslash_tma<EPI, NSUM, Fin><<<grid, T * sh.G, smem, c.stream>>>(fat, lng, a, fin, T, Rr);
+      timing_end(family);
+      MKS_CUDA(cudaGetLastError());
+      return MKS_OK;
+    }
+  }
   switch (sh.NB) {
   case 1: return launch_dslash_nb<R, LinkT, InT, OutT, 1, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block);
   case 2: return launch_dslash_nb<R, LinkT, InT, OutT, 2, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block);
@@ -472,7 +525,7 @@ static int tune_shape(const LinkT &fat, const LinkT &lng, int nsrc, Shape *best)
       const int NB = nbs[ib];
       if (G * NB < nsrc || G * NB > MAXSRC || (G * NB >= 2 * nsrc && G * NB > 1)) continue;
       for (int block = 128; block <= 256; block *= 2) {
-        Shape sh = {G, NB, block};
+        Shape sh = {G, NB, block, 0};
         float tot = 0;
         for (int it = 0; it < 4; it++) {
           MKS_CUDA(cudaEventRecord(e0, c.stream));
@@ -488,6 +541,28 @@ static int tune_shape(const LinkT &fat, const LinkT &lng, int nsrc, Shape *best)
       }
     }
   }
+  if constexpr (std::is_same<LinkT, LinkF32>::value) {
+    // the TMA-staged kernel: one source per thread, G = nsrc rounded up to a power of two
+    int G = 1;
+    while (G < nsrc) G *= 2;
+    int T, Rr;
+    if (nsrc >= 2 && tma_tile(c.geom, G, &T, &Rr)) {
+      Shape sh = {G, 1, T * G, 1};
+      float tot = 0;
+      for (int it = 0; it < 4; it++) {
+        MKS_CUDA(cudaEventRecord(e0, c.stream));
+        MKS_TRY((launch_shape<R, LinkT, InT, OutT, EPI, (EPI == EPI_AXPY ? 3 : 0)>(MKS_K_TUNE, fat, lng, a, NoFinish(),
+                                                                                    sh)));
+        MKS_CUDA(cudaEventRecord(e1, c.stream));
+        MKS_CUDA(cudaEventSynchronize(e1));
+        float ms;
+        MKS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (it > 0) tot += ms;
+      }
+      MKS_TRY(red_check());
+      if (tot < best_ms) { best_ms = tot; *best = sh; }
+    }
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return MKS_OK;
@@ -495,7 +570,9 @@ static int tune_shape(const LinkT &fat, const LinkT &lng, int nsrc, Shape *best)
 
 // MKS_SHAPE="prec:nsrc:G:NB:block[,...]" fixes shapes by hand (a tuning
 // cache written by the user); entries must satisfy G*NB >= nsrc, G*NB <= 16,
-// NB in {1,2,4,8}, G a power of two, block in {128,256}.
+// NB in {1,2,4,8}, G a power of two, block in {128,256}.  The entry
+// "prec:nsrc:G:1:tma" (prec 1, FP32) selects the TMA-staged kernel with G
+// threads per site, where the lattice admits its tiles.
 static bool shape_override(int prec, int nsrc, Shape *out) {
   const char *e = getenv("MKS_SHAPE");
   if (!e) return false;
@@ -504,11 +581,19 @@ static bool shape_override(int prec, int nsrc, Shape *out) {
   while (pos < str.size()) {
     size_t end = str.find(',', pos);
     if (end == std::string::npos) end = str.size();
+    const std::string item = str.substr(pos, end - pos);
     int p, n, G, NB, B;
-    if (sscanf(str.substr(pos, end - pos).c_str(), "%d:%d:%d:%d:%d", &p, &n, &G, &NB, &B) == 5 && p == prec &&
+    if (sscanf(item.c_str(), "%d:%d:%d:%d:%d", &p, &n, &G, &NB, &B) == 5 && p == prec &&
         n == nsrc && G >= 1 && G <= 16 && (G & (G - 1)) == 0 && (NB == 1 || NB == 2 || NB == 4 || NB == 8) &&
         G * NB >= nsrc && G * NB <= MAXSRC && (B == 128 || B == 256)) {
-      *out = {G, NB, B};
+      *out = {G, NB, B, 0};
+      return true;
+    }
+    int T, Rr;
+    if (sscanf(item.c_str(), "%d:%d:%d:%d:", &p, &n, &G, &NB) == 4 && item.size() > 4 &&
+        item.compare(item.size() - 4, 4, ":tma") == 0 && p == MKS_PREC_SINGLE && p == prec && n == nsrc &&
+        NB == 1 && G >= nsrc && G <= 16 && (G & (G - 1)) == 0 && tma_tile(ctx().geom, G, &T, &Rr)) {
+      *out = {G, 1, T * G, 1};
       return true;
     }
     pos = end + 1;
@@ -802,49 +887,31 @@ template <typename T> static void key_push(std::vector<uint64_t> &k, const T &v)
 
 static int cg_iteration(const LinkSlot &sl, int par, int nsrc, int prec, const double *msq4, CgFields &f, Solver &S);
 
-static int run_batch(const LinkSlot &sl, int par, int nsrc, int prec, const double *msq4, CgFields &f, Solver &S,
-                     int np) {
+// Run `issue` (a batch of launches on the context stream) through the graph
+// cache: eagerly the first time a key is seen, captured and instantiated the
+// second time, replayed afterwards.  The key must hold every pointer and
+// scalar the launches bake in.
+template <class F>
+static int graph_batch(const std::vector<uint64_t> &key, F issue) {
   Context &c = ctx();
-  if (!graphs_enabled()) {
-    for (int k = 0; k < np; k++) MKS_TRY(cg_iteration(sl, par, nsrc, prec, msq4, f, S));
-    return MKS_OK;
-  }
-  std::vector<uint64_t> key;
-  key_push(key, nsrc); key_push(key, prec); key_push(key, par); key_push(key, np); key_push(key, (int)c.timing);
-  key_push(key, c.geom.Vh); key_push(key, c.geom.nx); key_push(key, c.geom.ny); key_push(key, c.geom.nz);
-  key_push(key, c.geom.nt);
-  key_push(key, sl.fat64); key_push(key, sl.lng64); key_push(key, sl.fat32a); key_push(key, sl.lng32a);
-  key_push(key, sl.fat32b); key_push(key, sl.lng32b); key_push(key, sl.fat16a); key_push(key, sl.lng16a);
-  key_push(key, sl.fat16b); key_push(key, sl.lng16b); key_push(key, sl.fat16scale); key_push(key, sl.lng16scale);
-  key_push(key, S.st); key_push(key, S.skip); key_push(key, c.red.partials); key_push(key, c.red.count);
-  for (int s = 0; s < nsrc; s++) {
-    key_push(key, msq4[s]);
-    key_push(key, f.x[s]); key_push(key, f.p[s]); key_push(key, f.r[s]); key_push(key, f.ttt[s]); key_push(key, f.t[s]);
-    key_push(key, f.x32[s]); key_push(key, f.p32[s]); key_push(key, f.r32[s]); key_push(key, f.ttt32[s]);
-    key_push(key, f.t32[s]); key_push(key, f.p16[s]); key_push(key, f.t16[s]); key_push(key, f.p16n[s]);
-    key_push(key, f.t16n[s]);
-  }
+  if (!graphs_enabled()) return issue();
   GraphEntry *e = nullptr;
   for (auto &g : g_graphs)
     if (g.key == key) { e = &g; break; }
   if (!e) {
-    if (g_graphs.size() >= 8) { free_graph(g_graphs.front()); g_graphs.erase(g_graphs.begin()); }
+    if (g_graphs.size() >= 32) { free_graph(g_graphs.front()); g_graphs.erase(g_graphs.begin()); }
     g_graphs.emplace_back();
     e = &g_graphs.back();
     e->key = key;
   }
   if (!e->exec) {
-    if (e->seen++ == 0) {
-      for (int k = 0; k < np; k++) MKS_TRY(cg_iteration(sl, par, nsrc, prec, msq4, f, S));
-      return MKS_OK;
-    }
+    if (e->seen++ == 0) return issue();
     Capture cap;
     cap.timed = c.timing;
     c.capture = &cap;
     int rc = MKS_OK;
     cudaError_t e0 = cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeRelaxed);
-    if (e0 == cudaSuccess)
-      for (int k = 0; k < np && rc >= 0; k++) rc = cg_iteration(sl, par, nsrc, prec, msq4, f, S);
+    if (e0 == cudaSuccess) rc = issue();
     cudaGraph_t graph = nullptr;
     cudaError_t e1 = e0 == cudaSuccess ? cudaStreamEndCapture(c.stream, &graph) : e0;
     c.capture = nullptr;
@@ -870,6 +937,32 @@ static int run_batch(const LinkSlot &sl, int par, int nsrc, int prec, const doub
   MKS_CUDA(cudaStreamSynchronize(c.stream));
   capture_account(e->cap);
   return MKS_OK;
+}
+
+static int run_batch(const LinkSlot &sl, int par, int nsrc, int prec, const double *msq4, CgFields &f, Solver &S,
+                     int np) {
+  Context &c = ctx();
+  auto issue = [&]() -> int {
+    for (int k = 0; k < np; k++) MKS_TRY(cg_iteration(sl, par, nsrc, prec, msq4, f, S));
+    return MKS_OK;
+  };
+  if (!graphs_enabled()) return issue();
+  std::vector<uint64_t> key;
+  key_push(key, nsrc); key_push(key, prec); key_push(key, par); key_push(key, np); key_push(key, (int)c.timing);
+  key_push(key, c.geom.Vh); key_push(key, c.geom.nx); key_push(key, c.geom.ny); key_push(key, c.geom.nz);
+  key_push(key, c.geom.nt);
+  key_push(key, sl.fat64); key_push(key, sl.lng64); key_push(key, sl.fat32a); key_push(key, sl.lng32a);
+  key_push(key, sl.fat32b); key_push(key, sl.lng32b); key_push(key, sl.fat16a); key_push(key, sl.lng16a);
+  key_push(key, sl.fat16b); key_push(key, sl.lng16b); key_push(key, sl.fat16scale); key_push(key, sl.lng16scale);
+  key_push(key, S.st); key_push(key, S.skip); key_push(key, c.red.partials); key_push(key, c.red.count);
+  for (int s = 0; s < nsrc; s++) {
+    key_push(key, msq4[s]);
+    key_push(key, f.x[s]); key_push(key, f.p[s]); key_push(key, f.r[s]); key_push(key, f.ttt[s]); key_push(key, f.t[s]);
+    key_push(key, f.x32[s]); key_push(key, f.p32[s]); key_push(key, f.r32[s]); key_push(key, f.ttt32[s]);
+    key_push(key, f.t32[s]); key_push(key, f.p16[s]); key_push(key, f.t16[s]); key_push(key, f.p16n[s]);
+    key_push(key, f.t16n[s]);
+  }
+  return graph_batch(key, issue);
 }
 
 // FP64 true residual r = src - (sigma - D D) x for the sources flagged
@@ -1752,8 +1845,10 @@ static int multishift_core(const LinkSlot &sl, int par, int prec, const double2 
   double *tot;
   MKS_TRY(wsv("ms_tot3", 4, &tot));
   int guard = 0;
-  while (h.status == ST_RUN) {
-    for (int k = 0; k < poll_interval(); k++) {
+  const int np = poll_interval();
+  // one batch of np iterations (3 launches each), replayed as a CUDA graph
+  auto issue = [&]() -> int {
+    for (int k = 0; k < np; k++) {
       if (prec == MKS_PREC_DOUBLE) {
         LinkSet64 L = links64(sl);
         DslashArgs<VecF64, VecF64, VecF64> a1;
@@ -1800,6 +1895,21 @@ static int multishift_core(const LinkSlot &sl, int par, int prec, const double2 
       up.r = r; up.ttt = ttt; up.cgp = cgp; up.p16 = p16; up.p16n = p16n; up.st = st; up.Vh = Vh;
       MKS_TRY((launch_site<OpShiftUpdate<R>, 1, FinMsUpdate>(MKS_K_SHIFT, up, FinMsUpdate{st, skip}, skip, 1)));
     }
+    return MKS_OK;
+  };
+  std::vector<uint64_t> key;
+  key_push(key, -1); key_push(key, sizeof(R)); key_push(key, prec); key_push(key, par); key_push(key, np);
+  key_push(key, (int)c.timing); key_push(key, c.geom.Vh); key_push(key, c.geom.nx); key_push(key, c.geom.ny);
+  key_push(key, c.geom.nz); key_push(key, c.geom.nt);
+  key_push(key, sl.fat64); key_push(key, sl.lng64); key_push(key, sl.fat32a); key_push(key, sl.lng32a);
+  key_push(key, sl.fat32b); key_push(key, sl.lng32b); key_push(key, sl.fat16a); key_push(key, sl.lng16a);
+  key_push(key, sl.fat16b); key_push(key, sl.lng16b); key_push(key, sl.fat16scale); key_push(key, sl.lng16scale);
+  key_push(key, st); key_push(key, skip); key_push(key, tot); key_push(key, c.red.partials); key_push(key, c.red.count);
+  key_push(key, h.shift0); key_push(key, nsh); key_push(key, r); key_push(key, cgp); key_push(key, ttt);
+  key_push(key, t); key_push(key, p16); key_push(key, t16); key_push(key, p16n); key_push(key, t16n);
+  for (int j = 0; j < nsh; j++) { key_push(key, psim[j]); key_push(key, pm[j]); }
+  while (h.status == ST_RUN) {
+    MKS_TRY(graph_batch(key, issue));
     MKS_CUDA(cudaMemcpyAsync(&h, st, sizeof h, cudaMemcpyDeviceToHost, c.stream));
     MKS_CUDA(cudaStreamSynchronize(c.stream));
     if (++guard > 10000000) return MKS_ERR_TIMEOUT;

@@ -138,3 +138,31 @@ def test_graph_replay_with_kernel_timing(gpu, oracle_cls):
     assert n.value > 3 * 2 * 20 and t.value > 0
     # replayed solves give the same answer as the eager first one
     assert rel(xs[2], xs[0]) < 1e-12 and rel(xs[1], xs[0]) < 1e-12
+
+
+@pytest.mark.parametrize("nsrc", [5, 8, 16])
+def test_block_cg_tma_staged_links(gpu, oracle_cls, monkeypatch, nsrc):
+    """The FP32 multi-source D_eo whose links are staged per tile in shared
+    memory by TMA bulk copies (shape forced through MKS_SHAPE; a lattice no
+    other test uses, so the shape is chosen afresh): every source reaches the
+    oracle's solution, and the shape in use is the staged kernel's (block =
+    tile sites x G threads per site: 24 x 8 or 16 x 16 here)."""
+    import ctypes
+    m = gpu
+    dims = (8, 12, 8, 8)
+    G = 8 if nsrc <= 8 else 16
+    monkeypatch.setenv("MKS_SHAPE", "1:%d:%d:1:tma" % (nsrc, G))
+    m.set_lattice((4, 4, 4, 4))   # a lattice change drops the shapes chosen earlier
+    orc, fat, lng = _setup(m, oracle_cls, dims)
+    srcs = [m.gen_vector(dims, 500 + k, m.EVEN) for k in range(nsrc)]
+    xs = [np.zeros_like(s) for s in srcs]
+    qic = m.QuarkInvertControl(resid=1e-10, max=2000, nrestart=5, parity=m.EVEN, prec=m.PREC_SINGLE)
+    it, per = m.ks_congrad_block_parity(srcs, xs, qic, 0.03)
+    Gq, nb, block = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    m.check(m._lib.load().mks_tuned_shape(m.PREC_SINGLE, nsrc, ctypes.byref(Gq), ctypes.byref(nb),
+                                          ctypes.byref(block)), "mks_tuned_shape")
+    assert (Gq.value, nb.value, block.value) == (G, 1, 24 * 8 if G == 8 else 16 * 16)
+    for k in range(nsrc):
+        assert per[k].converged == 1
+        _, xo, _ = orc.congrad(fat, lng, srcs[k], np.zeros_like(srcs[k]), 0.03, m.EVEN, 1e-13, 0.0, 2000, 5)
+        assert rel(xs[k], xo) < 1e-7, (k, rel(xs[k], xo))
