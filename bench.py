@@ -134,8 +134,7 @@ def cpu_baseline(sample_iters=20, threads=None):
 
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the multi-source
 # D_eo family (mean of the plain D and the fused CG-epilogue launch), from
-# ncu captures of this benchmark on GB300 (profiles/k_dslash_f32_nsrc8_32c64_full.md
-# for 8 sources, profiles/k_dslash_f32_nsrc8_32c64_dram.md for 4)
+# ncu captures of this benchmark on GB300 (summaries under profiles/)
 MEASURED_TRAFFIC = {
     ("single", 8, (32, 32, 32, 64)): 0.5 * (1.802e9 + 2.418e9),
     ("single", 4, (32, 32, 32, 64)): 0.5 * (1.520e9 + 1.722e9),

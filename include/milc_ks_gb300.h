@@ -45,7 +45,7 @@ extern "C" {
 #define MKS_ERR_STATE      -4   /* library not initialised / lattice or links not loaded */
 #define MKS_ERR_TIMEOUT    -5   /* a bounded device-side wait gave up */
 #define MKS_ERR_NUMERIC    -6   /* NaN/Inf met in a solver recurrence */
-#define MKS_ERR_UNSUPPORTED -7  /* option not provided by this build */
+#define MKS_ERR_UNSUPPORTED -7  /* option not provided by the library */
 
 /* ---- parities: same values as MILC include/macros.h:17-19 ---- */
 #define MKS_ODD        0x01
@@ -171,8 +171,11 @@ int mks_mat_invert_block_uml(int nsrc, const double *const *src, double *const *
  * 38-250; CPU semantics generic_ks/ks_multicg_offset.c:63-505).  Stops
  * when the smallest shift meets arg->resid, like the CPU code (:381).
  * psim is overwritten (zero initial guess).  res has num_offsets entries.
- * arg->prec selects FP64, or FP32/FP16 shifted updates followed by an FP64
- * refinement of every shift (generic_ks/ks_multicg.c:170-228). */
+ * arg->prec selects FP64, or FP32/FP16 shifted updates with FP64 reliable
+ * updates of the lowest shift (every shift's solution accumulated in FP64),
+ * an FP64 true-residual check of every shift, and a mixed-precision
+ * refinement of the shifts that miss arg->resid (generic_ks/ks_multicg.c:
+ * 170-228). */
 int mks_ks_multicg_offset_field(const double *src, double *const *psim,
                                 const double *offsets, int num_offsets, int slot,
                                 const mks_invert_arg *arg, mks_invert_result *res);

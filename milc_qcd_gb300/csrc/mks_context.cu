@@ -363,7 +363,7 @@ int mks_init(int device) {
   cudaDeviceProp prop;
   MKS_CUDA(cudaGetDeviceProperties(&prop, device));
   if (prop.major < 10) {
-    snprintf(g_errmsg, sizeof g_errmsg, "device %d is sm_%d%d; this build targets sm_103a", device,
+    snprintf(g_errmsg, sizeof g_errmsg, "device %d is sm_%d%d; the library is compiled for sm_103a", device,
              prop.major, prop.minor);
     return MKS_ERR_UNSUPPORTED;
   }

@@ -1,6 +1,6 @@
 /* milc_oracle.h -- CPU restatement of MILC's improved-staggered hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This is the checker the CUDA path is compared
+ * TEST INFRASTRUCTURE ONLY.  This is the oracle the CUDA path is compared
  * against (tests, the smoke check and the CPU-baseline leg of the
  * benchmark); the product library never links or calls it.
  *

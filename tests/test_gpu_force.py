@@ -1,7 +1,7 @@
 """HISQ fermion force on the GPU against the oracle, which is itself pinned
 to MILC's eo_fermion_force_multi (tests/test_oracle_golden.py) and to
 central finite differences of the action (tests/test_oracle_force.py).
-Spec tolerance: 1e-10 relative."""
+Required tolerance: 1e-10 relative."""
 import numpy as np
 import pytest
 
