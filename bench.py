@@ -350,6 +350,19 @@ def gpu_arm(args):
     x_host = [t.cpu().numpy() for t in d_dst]
     final_rsq = max(res[k].final_rsq for k in range(N))
     converged = all(res[k].converged for k in range(N))
+    sum_iters = sum(res[k].final_iters for k in range(N))
+    # sustained solver rate in MILC's count (1187 flop per site per CG
+    # iteration, d_congrad5_fn_milc.c:82)
+    cg_gflops = 1187.0 * (V // 2) * sum_iters / (step_ms * 1e-3) / 1e9
+    # each source's solution against the plain FP64 GPU CG's solution of the
+    # same system (outside the timed region)
+    sol_err = []
+    for k in range(N):
+        d64k = torch.zeros_like(d_src[k])
+        m.check(lib.mks_ks_congrad_parity_dev(d_src[k].data_ptr(), d64k.data_ptr(), MASS, 0,
+                                              ctypes.byref(arg64), ctypes.byref(_lib.InvertResult())), "fp64 ref")
+        xr = d64k.cpu().numpy()[:V // 2]
+        sol_err.append(float(np.linalg.norm(x_host[k][:V // 2] - xr) / np.linalg.norm(xr)))
     # kernel roofline: the sloppy D_eo (dominant kernel), live CUDA-event timing
     fam = {m.PREC_HALF: 2, m.PREC_SINGLE: 1, m.PREC_DOUBLE: 0}[prec]
     if N > 1 and prec != m.PREC_DOUBLE:
@@ -412,6 +425,8 @@ def gpu_arm(args):
         "fp64_plain_single_rhs": {"s_per_solve": t_fp64, "iters": it64, "final_rsq": res64.final_rsq},
         "speedup_vs_fp64_plain": t_fp64 / per_src,
         "iters": iters, "reliable_updates": reliable, "final_rsq_max": final_rsq, "converged": converged,
+        "cg_gflops": cg_gflops,
+        "solution_rel_error_vs_fp64_cg": sol_err,
         "dslash_gbs": {"f32_single_rhs": gbs32, "f32_ms": ms32.value, "f64_ms": ms64.value,
                        "f64_gflops": 1146.0 * Vh / (ms64.value * 1e-3) / 1e9},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
