@@ -500,6 +500,58 @@ def rhmc_workload(args):
     print(json.dumps(line), flush=True)
 
 
+# HISQ link rebuild + fermion force of one molecular-dynamics step of the
+# 2+1+1 workload: 38 rational-function terms (16 light + 12 strange in the
+# eps = 0 Naik group, 10 charm in the eps_naik(0.432) group), seeded
+# synthetic links and solutions; once in FP64 and once in the FP32 setting.
+def force_workload(args):
+    import milc_qcd_gb300 as m
+    from milc_qcd_gb300.remez import eps_naik
+    dims = tuple(args.dims) if args.dims else (48, 48, 48, 96)
+    V = int(np.prod(dims))
+    m.init(0)
+    m.set_lattice(dims)
+    lib = m._lib.load()
+    m.gauge_load(m.gen_thin_links(dims, 7, 0.2))
+    eps = (0.0, eps_naik(0.432))
+    rng = np.random.default_rng(3)
+    nterms, orders = 38, [28, 10]
+    xxx = [rng.standard_normal((V, 6)) for _ in range(nterms)]
+    res = rng.uniform(0.01, 0.1, nterms)
+    mom = np.zeros((V, 4, 10))
+    out = {}
+    runs = {"both": (("f64", m.PREC_DOUBLE), ("f32", m.PREC_SINGLE)), "double": (("f64", m.PREC_DOUBLE),),
+            "single": (("f32", m.PREC_SINGLE),)}[args.md_prec]
+    for name, prec in runs:
+        m.md_precision(prec)
+        per = []
+        for rep_ in range(max(args.warmup, 0) + max(args.steps, 1)):
+            lib.mks_timing_reset()
+            lib.mks_timing_enable(1)
+            t0 = time.time()
+            m.rebuild_links("hisq", eps)
+            t1 = time.time()
+            m.eo_fermion_force_multi(0.1, res, xxx, mom, n_orders_naik=orders, n_naiks=2)
+            t2 = time.time()
+            lib.mks_timing_enable(0)
+            fam = {}
+            for fname, k in m._lib.KERNEL_FAMILIES.items():
+                t, n = ctypes.c_double(), ctypes.c_longlong()
+                lib.mks_timing_get(k, ctypes.byref(t), ctypes.byref(n))
+                if n.value:
+                    fam[fname] = {"ms": t.value, "launches": n.value}
+            per.append({"links_s": t1 - t0, "force_s_incl_host_copies": t2 - t1, "kernel": fam})
+        out[name] = per[-1]
+    m.md_precision(m.PREC_DOUBLE)
+    line = {"metric": "HISQ link rebuild + fermion force, s per molecular-dynamics step (%s)" % "x".join(map(str, dims)),
+            "value": sum(out[k]["links_s"] + out[k]["force_s_incl_host_copies"] for k in list(out)[-1:]),
+            "unit": "s/step", "n_gpus": 1,
+            "higher_is_better": False, "dtype": "f32+f64", "data": "synthetic (seeded exp(i 0.2 H) links, Gaussian solutions)",
+            "config": {"workload": "HISQ links (2 Naik groups) + fermion force, 38 terms", "lattice": list(dims)},
+            "runs": out}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -515,14 +567,18 @@ def main():
     ap.add_argument("--ref-iters", type=int, default=int(os.environ.get("MKS_REF_ITERS", "0")) or None)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
-    ap.add_argument("--workload", default="cg", choices=["cg", "rhmc"],
-                    help="cg: the headline CG benchmark; rhmc: one 2+1+1 HISQ RHMC trajectory")
+    ap.add_argument("--md-prec", default="both", choices=["both", "single", "double"],
+                    help="force workload: the molecular-dynamics precisions to run")
+    ap.add_argument("--workload", default="cg", choices=["cg", "rhmc", "force"],
+                    help="cg: the headline CG benchmark; rhmc: one 2+1+1 HISQ RHMC trajectory; "
+                         "force: HISQ link rebuild + fermion force of one molecular-dynamics step")
     args = ap.parse_args()
-    if args.workload == "rhmc":
+    if args.workload in ("rhmc", "force"):
         if args.impl == "reference":
-            print(json.dumps({"impl": "reference", "unavailable": "the rhmc workload has no CPU reference arm"}))
+            print(json.dumps({"impl": "reference", "unavailable": "the %s workload has no CPU reference arm"
+                              % args.workload}))
             return
-        rhmc_workload(args)
+        (rhmc_workload if args.workload == "rhmc" else force_workload)(args)
         return
     if args.dims:
         global DIMS
