@@ -63,7 +63,7 @@ void orc_rephase(const orc_lat *L, double *links) {
   }
 }
 
-/* ---------------- SU(3) primitives (libraries/*.c semantics) ---------------- */
+/* ---------------- SU(3) primitives (semantics of MILC's libraries/ directory) ---------------- */
 #define RE(m, i, j) (m)[2 * (3 * (i) + (j))]
 #define IM(m, i, j) (m)[2 * (3 * (i) + (j)) + 1]
 
@@ -298,7 +298,7 @@ int orc_multicg_offset(const orc_lat *L, const double *fat, const double *lng,
   par_range(L, parity, &lo, &hi);
   int otherparity = parity == ORC_EVEN ? ORC_ODD : ORC_EVEN;
   size_t n6 = 6 * L->V;
-  if (num_offsets == 0) return 0;
+  if (num_offsets <= 0) return 0;
   double *shifts = (double *)malloc(num_offsets * sizeof(double));
   double *zeta_i = (double *)malloc(num_offsets * sizeof(double));
   double *zeta_im1 = (double *)malloc(num_offsets * sizeof(double));
@@ -316,6 +316,7 @@ int orc_multicg_offset(const orc_lat *L, const double *fat, const double *lng,
     shifts[j] = offsets[j];
     if (offsets[j] < offset_low) { offset_low = offsets[j]; j_low = j; }
   }
+  if (j_low < 0) j_low = 0;  /* offsets >= 1e20: keep the first as the base */
   for (int j = 0; j < num_offsets; j++) if (j != j_low) shifts[j] -= shifts[j_low];
   double shift0 = -shifts[j_low];
   double source_norm = 0;
