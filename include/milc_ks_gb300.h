@@ -201,7 +201,9 @@ int mks_get_hisq_aux(double *V, double *W);
 /* Number of links in the last HISQ construction for which MILC's
    HISQ_REUNIT_ALLOW_SVD criteria (relative 1e-8 / absolute 1e-8 on det V^dag V,
    generic_ks/su3_mat_op.c:1037-1080) would have switched to its SVD branch;
-   the analytic projection was used for them.  Returns a count >= 0. */
+   the analytic projection was used for them.  Returns a count >= 0; 0 after
+   a construction in the FP32 molecular-dynamics precision, where the test
+   is below the arithmetic's resolution and is not made. */
 int mks_hisq_reunit_svd_count(void);
 /* Rebuild the fat/long links of slots 0..n_naiks-1 from the thin links
  * already resident on the device (after mks_update_u / mks_reunitarize or
@@ -351,11 +353,11 @@ int mks_reunitarize(void);
 int mks_plaquette(double *ss, double *st);
 /* Precision of later link constructions (mks_load_links_from_thin,
  * mks_rebuild_links) and fermion forces: MKS_PREC_DOUBLE (the default,
- * MILC's double build) or MKS_PREC_SINGLE (for molecular-dynamics forces:
- * the smearing stages, staples and force adjoints stored and multiplied in
- * FP32; the U(3) projection and its adjoint in FP64 arithmetic; the
+ * MILC's double build) or MKS_PREC_SINGLE (for molecular-dynamics forces,
+ * like MILC's single-precision build: the smearing stages, the U(3)
+ * projection, staples and force adjoints stored and computed in FP32; the
  * resident links, the slots' fat / long links and the momentum update stay
- * FP64 fields).  No reference counterpart: MILC's CPU force is FP64. */
+ * FP64 fields).  No reference counterpart in MILC's double build. */
 int mks_md_precision(int prec);
 
 /* ------------------------------------------------------------------ */

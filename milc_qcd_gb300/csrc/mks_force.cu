@@ -179,7 +179,9 @@ __global__ void __launch_bounds__(128) k_naik_adj(Geom g, const typename Stor<R>
 //   K_V = R K_W + (N + N^dag) V^dag,  M = K_W V,
 //   N = sum_i tr(M Q^i) Psi_i + f1 M + f2 (Q M + M Q),
 //   Psi_i = df_i/du R/2 + df_i/dv (u R - 1)/2 + df_i/dw (w/2) R^2.
-// Always FP64 arithmetic (eigenvalues, 1/D); K_W and K_V stored in precision S.
+// Arithmetic and the storage of K_W, K_V in precision S (MILC's own
+// single-precision build runs this derivative in float too); V is the
+// resident FP64 field.
 template <typename S>
 __global__ void __launch_bounds__(128) k_unit_adj(Geom g, const double2 *Vl, const typename Stor<S>::t *KW,
                                                   typename Stor<S>::t *KV, unsigned int *nfilter) {
@@ -190,72 +192,72 @@ __global__ void __launch_bounds__(128) k_unit_adj(Geom g, const double2 *Vl, con
   if (h >= Vh) return;
   MatF Vm = link_dir((double2 *)Vl, mu, Vh);
   MatT<S> Kw = link_dir((T2 *)KW, mu, Vh), Kv = link_dir(KV, mu, Vh);
-  const M3<double> V = Vm.ld(par, h, Vh);
-  M3<double> Q = mm_an(V, V), Q2 = mm_nn(Q, Q);
-  double c0 = Q.e[0][0].re + Q.e[1][1].re + Q.e[2][2].re;
-  double c1 = (Q2.e[0][0].re + Q2.e[1][1].re + Q2.e[2][2].re) / 2;
-  double q3 = 0;
+  const M3<S> V = from64<S>(Vm.ld(par, h, Vh));
+  M3<S> Q = tan_<S>(V, V), Q2 = tnn<S>(Q, Q);
+  S c0 = Q.e[0][0].re + Q.e[1][1].re + Q.e[2][2].re;
+  S c1 = (Q2.e[0][0].re + Q2.e[1][1].re + Q2.e[2][2].re) / 2;
+  S q3 = 0;
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int k = 0; k < 3; k++) q3 += Q2.e[i][k].re * Q.e[k][i].re - Q2.e[i][k].im * Q.e[k][i].im;
-  double c2 = q3 / 3, gv[3];
-  double Sv = c1 / 3 - c0 * (c0 / 18);
-  if (fabs(Sv) < 1.0e-14) {
+  S c2 = q3 / 3, gv[3];
+  S Sv = c1 / 3 - c0 * (c0 / 18);
+  if (fabs(Sv) < (S)1.0e-14) {
     gv[0] = gv[1] = gv[2] = c0 / 3;
   } else {
-    double Rr = c2 / 2 - c0 * (c1 / 3) + c0 * c0 * (c0 / 27);
+    S Rr = c2 / 2 - c0 * (c1 / 3) + c0 * c0 * (c0 / 27);
     Sv = sqrt(Sv);
-    double RoS = Rr / (Sv * Sv * Sv), theta;
-    if (!(fabs(RoS) < 1.0)) theta = Rr > 0 ? 0.0 : 3.14159265358979323846264338328;
+    S RoS = Rr / (Sv * Sv * Sv), theta;
+    if (!(fabs(RoS) < (S)1)) theta = Rr > 0 ? (S)0 : (S)3.14159265358979323846264338328;
     else theta = acos(RoS);
-    double th3 = theta / 3, pi23 = 6.28318530717958647692528676656 / 3;
+    S th3 = theta / 3, pi23 = (S)(6.28318530717958647692528676656 / 3);
     gv[0] = c0 / 3 + 2 * Sv * cos(th3);
     gv[1] = c0 / 3 + 2 * Sv * cos(th3 + pi23);
     gv[2] = c0 / 3 + 2 * Sv * cos(th3 + 2 * pi23);
   }
-  double gmin = fmin(gv[0], fmin(gv[1], gv[2]));
-  if (gmin < 5.0e-5) {  // HISQ_FORCE_FILTER
+  S gmin = fmin(gv[0], fmin(gv[1], gv[2]));
+  if (gmin < (S)5.0e-5) {  // HISQ_FORCE_FILTER
     if (nfilter) atomicAdd(nfilter, 1u);
-    for (int a = 0; a < 3; a++) gv[a] += 5.0e-5;
-    for (int i = 0; i < 3; i++) Q.e[i][i].re += 5.0e-5;
-    Q2 = mm_nn(Q, Q);
+    for (int a = 0; a < 3; a++) gv[a] += (S)5.0e-5;
+    for (int i = 0; i < 3; i++) Q.e[i][i].re += (S)5.0e-5;
+    Q2 = tnn<S>(Q, Q);
   }
-  const double s0 = sqrt(gv[0]), s1 = sqrt(gv[1]), s2 = sqrt(gv[2]);
-  const double u = s0 + s1 + s2, v = s0 * s1 + s0 * s2 + s1 * s2, w = s0 * s1 * s2;
-  const double D = w * (u * v - w);
-  const double f0 = (u * v * v - w * (u * u + v)) / D, f1 = (2 * u * v - w - u * u * u) / D, f2 = u / D;
-  const double Du = v * w, Dv = u * w, Dw = u * v - 2 * w;
-  double fu[3], fv[3], fw[3];
+  const S s0 = sqrt(gv[0]), s1 = sqrt(gv[1]), s2 = sqrt(gv[2]);
+  const S u = s0 + s1 + s2, v = s0 * s1 + s0 * s2 + s1 * s2, w = s0 * s1 * s2;
+  const S D = w * (u * v - w);
+  const S f0 = (u * v * v - w * (u * u + v)) / D, f1 = (2 * u * v - w - u * u * u) / D, f2 = u / D;
+  const S Du = v * w, Dv = u * w, Dw = u * v - 2 * w;
+  S fu[3], fv[3], fw[3];
   fu[0] = (v * v - 2 * u * w) / D - f0 * Du / D;
   fv[0] = (2 * u * v - w) / D - f0 * Dv / D;
   fw[0] = (-u * u - v) / D - f0 * Dw / D;
   fu[1] = (2 * v - 3 * u * u) / D - f1 * Du / D;
   fv[1] = (2 * u) / D - f1 * Dv / D;
-  fw[1] = -1.0 / D - f1 * Dw / D;
-  fu[2] = 1.0 / D - f2 * Du / D;
+  fw[1] = (S)-1 / D - f1 * Dw / D;
+  fu[2] = (S)1 / D - f2 * Du / D;
   fv[2] = -f2 * Dv / D;
   fw[2] = -f2 * Dw / D;
-  M3<double> R;
+  M3<S> R;
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = 0; j < 3; j++) {
-      R.e[i][j].re = f1 * Q.e[i][j].re + f2 * Q2.e[i][j].re + (i == j ? f0 : 0.0);
+      R.e[i][j].re = f1 * Q.e[i][j].re + f2 * Q2.e[i][j].re + (i == j ? f0 : (S)0);
       R.e[i][j].im = f1 * Q.e[i][j].im + f2 * Q2.e[i][j].im;
     }
-  const M3<double> R2 = mm_nn(R, R);
-  const M3<double> Kwv = to64<S>(Kw.ld(par, h, Vh));
-  const M3<double> M = mm_nn(Kwv, V);
-  const M3<double> QM = mm_nn(Q, M), MQ = mm_nn(M, Q), MQ2 = mm_nn(M, Q2);
-  cplx<double> tr[3] = {{0, 0}, {0, 0}, {0, 0}};
+  const M3<S> R2 = tnn<S>(R, R);
+  const M3<S> Kwv = Kw.ld(par, h, Vh);
+  const M3<S> M = tnn<S>(Kwv, V);
+  const M3<S> QM = tnn<S>(Q, M), MQ = tnn<S>(M, Q), MQ2 = tnn<S>(M, Q2);
+  cplx<S> tr[3] = {{0, 0}, {0, 0}, {0, 0}};
 #pragma unroll
   for (int a = 0; a < 3; a++) {
     tr[0].re += M.e[a][a].re; tr[0].im += M.e[a][a].im;
     tr[1].re += MQ.e[a][a].re; tr[1].im += MQ.e[a][a].im;
     tr[2].re += MQ2.e[a][a].re; tr[2].im += MQ2.e[a][a].im;
   }
-  M3<double> N;
+  M3<S> N;
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -265,18 +267,18 @@ __global__ void __launch_bounds__(128) k_unit_adj(Geom g, const double2 *Vl, con
     }
 #pragma unroll
   for (int k = 0; k < 3; k++) {
-    const double cu = 0.5 * fu[k] + 0.5 * fv[k] * u, cw = 0.5 * fw[k] * w, cd = -0.5 * fv[k];
+    const S cu = (S)0.5 * fu[k] + (S)0.5 * fv[k] * u, cw = (S)0.5 * fw[k] * w, cd = (S)-0.5 * fv[k];
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
       for (int j = 0; j < 3; j++) {
-        double pr = cu * R.e[i][j].re + cw * R2.e[i][j].re + (i == j ? cd : 0.0);
-        double pi = cu * R.e[i][j].im + cw * R2.e[i][j].im;
+        S pr = cu * R.e[i][j].re + cw * R2.e[i][j].re + (i == j ? cd : (S)0);
+        S pi = cu * R.e[i][j].im + cw * R2.e[i][j].im;
         N.e[i][j].re += tr[k].re * pr - tr[k].im * pi;
         N.e[i][j].im += tr[k].re * pi + tr[k].im * pr;
       }
   }
-  M3<double> Nh;
+  M3<S> Nh;
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -284,9 +286,9 @@ __global__ void __launch_bounds__(128) k_unit_adj(Geom g, const double2 *Vl, con
       Nh.e[i][j].re = N.e[i][j].re + N.e[j][i].re;
       Nh.e[i][j].im = N.e[i][j].im - N.e[j][i].im;
     }
-  M3<double> out = mm_nn(R, Kwv);
-  macc<double>(out, mm_na(Nh, V), 1.0);
-  Kv.st(par, h, Vh, from64<S>(out));
+  M3<S> out = tnn<S>(R, Kwv);
+  macc<S>(out, tna<S>(Nh, V), (S)1);
+  Kv.st(par, h, Vh, out);
 }
 
 // 5. mom <- TA(mom + fac U K_U) in MILC's anti_hermitmat layout, device AoS [V][4][10]

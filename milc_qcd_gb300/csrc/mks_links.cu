@@ -70,69 +70,72 @@ __global__ void __launch_bounds__(128) k_naik(Geom g, const typename Stor<R>::t 
 
 // W = V (V^dag V)^(-1/2), analytic (u3_unitarize_analytic, generic_ks/su3_mat_op.c:828-1200).
 // Counts the links where MILC's HISQ_REUNIT_ALLOW_SVD criteria (1e-8) would
-// switch to its SVD branch.
-__device__ void u3_unitarize(const M3<double> &V, M3<double> &W, unsigned int *nsvd) {
-  M3<double> Q = mm_an(V, V), Q2 = mm_nn(Q, Q);
-  double c0 = Q.e[0][0].re + Q.e[1][1].re + Q.e[2][2].re;
-  double c1 = (Q2.e[0][0].re + Q2.e[1][1].re + Q2.e[2][2].re) / 2;
-  double q3 = 0;
+// switch to its SVD branch (in FP64 arithmetic).
+template <typename A>
+__device__ void u3_unitarize(const M3<A> &V, M3<A> &W, unsigned int *nsvd) {
+  M3<A> Q = tan_<A>(V, V), Q2 = tnn<A>(Q, Q);
+  A c0 = Q.e[0][0].re + Q.e[1][1].re + Q.e[2][2].re;
+  A c1 = (Q2.e[0][0].re + Q2.e[1][1].re + Q2.e[2][2].re) / 2;
+  A q3 = 0;
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int k = 0; k < 3; k++) q3 += Q2.e[i][k].re * Q.e[k][i].re - Q2.e[i][k].im * Q.e[k][i].im;
-  double c2 = q3 / 3;
-  double g0, g1, g2;
-  double S = c1 / 3 - c0 * (c0 / 18);
-  if (fabs(S) < 1.0e-14) {
+  A c2 = q3 / 3;
+  A g0, g1, g2;
+  A S = c1 / 3 - c0 * (c0 / 18);
+  if (fabs(S) < (A)1.0e-14) {
     g0 = g1 = g2 = c0 / 3;
   } else {
-    double R = c2 / 2 - c0 * (c1 / 3) + c0 * c0 * (c0 / 27);
+    A R = c2 / 2 - c0 * (c1 / 3) + c0 * c0 * (c0 / 27);
     S = sqrt(S);
-    double RoS = R / (S * S * S), theta;
-    if (!(fabs(RoS) < 1.0)) theta = R > 0 ? 0.0 : 3.14159265358979323846264338328;
+    A RoS = R / (S * S * S), theta;
+    if (!(fabs(RoS) < (A)1)) theta = R > 0 ? (A)0 : (A)3.14159265358979323846264338328;
     else theta = acos(RoS);
-    double th3 = theta / 3, pi23 = 6.28318530717958647692528676656 / 3;
+    A th3 = theta / 3, pi23 = (A)(6.28318530717958647692528676656 / 3);
     g0 = c0 / 3 + 2 * S * cos(th3);
     g1 = c0 / 3 + 2 * S * cos(th3 + pi23);
     g2 = c0 / 3 + 2 * S * cos(th3 + 2 * pi23);
   }
-  // det V for the SVD criterion
-  {
-    const cplx<double>(*e)[3] = V.e;
-    cplx<double> a1 = {e[1][1].re * e[2][2].re - e[1][1].im * e[2][2].im - e[1][2].re * e[2][1].re + e[1][2].im * e[2][1].im,
+  // det V for the SVD criterion (FP64 constructions only: the 1e-8 relative
+  // test is below FP32 resolution)
+  if (sizeof(A) == 8) {
+    const cplx<A>(*e)[3] = V.e;
+    cplx<A> a1 = {e[1][1].re * e[2][2].re - e[1][1].im * e[2][2].im - e[1][2].re * e[2][1].re + e[1][2].im * e[2][1].im,
                        e[1][1].re * e[2][2].im + e[1][1].im * e[2][2].re - e[1][2].re * e[2][1].im - e[1][2].im * e[2][1].re};
-    cplx<double> a2 = {e[1][0].re * e[2][2].re - e[1][0].im * e[2][2].im - e[1][2].re * e[2][0].re + e[1][2].im * e[2][0].im,
+    cplx<A> a2 = {e[1][0].re * e[2][2].re - e[1][0].im * e[2][2].im - e[1][2].re * e[2][0].re + e[1][2].im * e[2][0].im,
                        e[1][0].re * e[2][2].im + e[1][0].im * e[2][2].re - e[1][2].re * e[2][0].im - e[1][2].im * e[2][0].re};
-    cplx<double> a3 = {e[1][0].re * e[2][1].re - e[1][0].im * e[2][1].im - e[1][1].re * e[2][0].re + e[1][1].im * e[2][0].im,
+    cplx<A> a3 = {e[1][0].re * e[2][1].re - e[1][0].im * e[2][1].im - e[1][1].re * e[2][0].re + e[1][1].im * e[2][0].im,
                        e[1][0].re * e[2][1].im + e[1][0].im * e[2][1].re - e[1][1].re * e[2][0].im - e[1][1].im * e[2][0].re};
-    double dre = e[0][0].re * a1.re - e[0][0].im * a1.im - e[0][1].re * a2.re + e[0][1].im * a2.im + e[0][2].re * a3.re - e[0][2].im * a3.im;
-    double dim = e[0][0].im * a1.re + e[0][0].re * a1.im - e[0][1].im * a2.re - e[0][1].re * a2.im + e[0][2].im * a3.re + e[0][2].re * a3.im;
-    double det = dre * dre + dim * dim;
-    bool svd = (det != 0 && fabs(det - g0 * g1 * g2) / fabs(det) > 1e-8) || det < 1e-8;
+    A dre = e[0][0].re * a1.re - e[0][0].im * a1.im - e[0][1].re * a2.re + e[0][1].im * a2.im + e[0][2].re * a3.re - e[0][2].im * a3.im;
+    A dim = e[0][0].im * a1.re + e[0][0].re * a1.im - e[0][1].im * a2.re - e[0][1].re * a2.im + e[0][2].im * a3.re + e[0][2].re * a3.im;
+    A det = dre * dre + dim * dim;
+    bool svd = (det != 0 && fabs(det - g0 * g1 * g2) / fabs(det) > (A)1e-8) || det < (A)1e-8;
     if (svd && nsvd) atomicAdd(nsvd, 1u);
   }
-  double g0sq = sqrt(g0), g1sq = sqrt(g1), g2sq = sqrt(g2);
-  double us = g1sq + g2sq, ws = g1sq * g2sq;
-  double vs = g0sq * us + ws;
+  A g0sq = sqrt(g0), g1sq = sqrt(g1), g2sq = sqrt(g2);
+  A us = g1sq + g2sq, ws = g1sq * g2sq;
+  A vs = g0sq * us + ws;
   us += g0sq;
   ws *= g0sq;
-  double denom = ws * (us * vs - ws);
-  double f0 = (us * vs * vs - ws * (us * us + vs)) / denom;
-  double f1 = (2 * us * vs - ws - us * us * us) / denom;
-  double f2 = us / denom;
-  M3<double> S2;
+  A denom = ws * (us * vs - ws);
+  A f0 = (us * vs * vs - ws * (us * us + vs)) / denom;
+  A f1 = (2 * us * vs - ws - us * us * us) / denom;
+  A f2 = us / denom;
+  M3<A> S2;
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = 0; j < 3; j++) {
-      S2.e[i][j].re = f1 * Q.e[i][j].re + f2 * Q2.e[i][j].re + (i == j ? f0 : 0.0);
+      S2.e[i][j].re = f1 * Q.e[i][j].re + f2 * Q2.e[i][j].re + (i == j ? f0 : (A)0);
       S2.e[i][j].im = f1 * Q.e[i][j].im + f2 * Q2.e[i][j].im;
     }
-  W = mm_nn(V, S2);
+  W = tnn<A>(V, S2);
 }
 
-// W = V (V^dag V)^(-1/2) for V stored in precision R, FP64 arithmetic; W
-// stored into W64 and (when given) Wr, V copied to V64 (when given)
+// W = V (V^dag V)^(-1/2) for V stored in precision R, arithmetic in R (MILC's
+// single-precision build projects in float too); W stored into W64 and
+// (when given) Wr, V copied to V64 (when given)
 template <typename R>
 __global__ void __launch_bounds__(128) k_unitarize(Geom g, const typename Stor<R>::t *Vl, double2 *V64, double2 *W,
                                                    typename Stor<R>::t *Wr, unsigned int *nsvd) {
@@ -142,23 +145,20 @@ __global__ void __launch_bounds__(128) k_unitarize(Geom g, const typename Stor<R
   if (h >= g.Vh) return;
   MatT<R> Vm = link_dir((T2 *)Vl, mu, g.Vh);
   MatF Wm = link_dir(W, mu, g.Vh);
-  M3<R> vr = Vm.ld(par, h, g.Vh);
-  M3<double> v, w;
+  const M3<R> v = Vm.ld(par, h, g.Vh);
+  M3<R> w;
+  u3_unitarize<R>(v, w, nsvd);
+  M3<double> w64, v64;
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
-    for (int j = 0; j < 3; j++) v.e[i][j] = {(double)vr.e[i][j].re, (double)vr.e[i][j].im};
-  u3_unitarize(v, w, nsvd);
-  Wm.st(par, h, g.Vh, w);
-  if (V64) link_dir(V64, mu, g.Vh).st(par, h, g.Vh, v);
-  if (Wr) {
-    M3<R> wr;
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-      for (int j = 0; j < 3; j++) wr.e[i][j] = {(R)w.e[i][j].re, (R)w.e[i][j].im};
-    link_dir(Wr, mu, g.Vh).st(par, h, g.Vh, wr);
-  }
+    for (int j = 0; j < 3; j++) {
+      w64.e[i][j] = {(double)w.e[i][j].re, (double)w.e[i][j].im};
+      v64.e[i][j] = {(double)v.e[i][j].re, (double)v.e[i][j].im};
+    }
+  Wm.st(par, h, g.Vh, w64);
+  if (V64) link_dir(V64, mu, g.Vh).st(par, h, g.Vh, v64);
+  if (Wr) link_dir(Wr, mu, g.Vh).st(par, h, g.Vh, w);
 }
 
 struct FatCoeffs { double one_link, naik, three_staple, five_staple, seven_staple, lepage; };
