@@ -182,6 +182,18 @@ int mks_ks_multicg_offset_field(const double *src, double *const *psim,
 int mks_ks_multicg_offset_field_dev(const double *src_dev, double *const *psim_dev,
                                     const double *offsets, int num_offsets, int slot,
                                     const mks_invert_arg *arg, mks_invert_result *res);
+/* Multi-shift CG for nf <= 4 fields (pseudofermion sources) on the same
+ * links, each with its own offsets: the same result as one
+ * mks_ks_multicg_offset_field_dev call per field (MILC calls
+ * ks_multicg_offset_field once per field, ks_imp_rhmc/ks_ratinv.c:108),
+ * with the fields' iterations batched: in FP32 (arg->prec MKS_PREC_SINGLE)
+ * one multi-source D_eo pair per iteration reads the links once for every
+ * running field.  offsets, psim_dev and res hold the fields' lists one after
+ * the other (num_offsets[f] entries each); device pointers.  Other
+ * precisions solve field by field.  Returns the largest iteration count. */
+int mks_ks_multicg_offset_multi_dev(int nf, const double *const *src_dev, const int *num_offsets,
+                                    const double *offsets, double *const *psim_dev, int slot,
+                                    const mks_invert_arg *arg, mks_invert_result *res);
 
 /* ------------------------------------------------------------------ */
 /* HISQ link construction.  Replaces load_hisq_aux_links_gpu and the fat /

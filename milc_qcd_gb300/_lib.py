@@ -68,6 +68,10 @@ SIGNATURES = {
     "mks_ks_multicg_offset_field_dev": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), DP,
                                                        ctypes.c_int, ctypes.c_int, ctypes.POINTER(InvertArg),
                                                        ctypes.POINTER(InvertResult)]),
+    "mks_ks_multicg_offset_multi_dev": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p),
+                                                       ctypes.POINTER(ctypes.c_int), DP,
+                                                       ctypes.POINTER(ctypes.c_void_p), ctypes.c_int,
+                                                       ctypes.POINTER(InvertArg), ctypes.POINTER(InvertResult)]),
     "mks_load_links_from_thin": (ctypes.c_int, [ctypes.c_int, DP, ctypes.c_int, DP, ctypes.c_double]),
     "mks_get_hisq_aux": (ctypes.c_int, [DP, DP]),
     "mks_hisq_reunit_svd_count": (ctypes.c_int, []),

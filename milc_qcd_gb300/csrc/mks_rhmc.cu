@@ -36,6 +36,7 @@ struct Traj {
   double *phi = nullptr;           // [n_pseudo][V][6]
   double *xs = nullptr;            // [max_terms][V][6] solutions (AoS)
   double *tmp = nullptr;           // [V][6]
+  double *gtmp = nullptr;          // [n_pseudo][V][6] heat-bath Gaussians
   double2 *xs_soa = nullptr;       // [max_terms][2][3][Vh] force input
   int max_terms = 0;
 
@@ -93,6 +94,62 @@ struct Traj {
     return MKS_OK;
   }
 
+  // fields of Naik group g (they share the links of slot g), in field order
+  std::vector<int> group(int g) const {
+    std::vector<int> fs;
+    for (int i = 0; i < p->n_pseudo; i++)
+      if (inaik[i] == g) fs.push_back(i);
+    return fs;
+  }
+
+  // ratinv for the fields fs of one Naik group (sources srcs[k], psim of
+  // field fs[k] into xs from x0[k] on).  In FP32 with equal residuals and
+  // iteration caps the fields' multi-shift solves run batched (one
+  // multi-source D_eo pair per iteration for all of them); otherwise one
+  // field after the other.
+  int ratinv_many(const std::vector<int> &fs, int tag, const std::vector<const double *> &srcs,
+                  const std::vector<int> &x0) {
+    bool batch = fs.size() >= 2 && fs.size() <= 4 && prec(tag) == MKS_PREC_SINGLE;
+    for (size_t k = 1; k < fs.size() && batch; k++)
+      batch = resid(fs[k], tag) == resid(fs[0], tag) && p->pf[fs[k]].max_cg == p->pf[fs[0]].max_cg;
+    if (!batch) {
+      for (size_t k = 0; k < fs.size(); k++) MKS_TRY(ratinv(srcs[k], fs[k], tag, x0[k]));
+      return MKS_OK;
+    }
+    MKS_TRY(links());
+    std::vector<int> ns;
+    std::vector<double> offs;
+    std::vector<double *> psim;
+    for (size_t k = 0; k < fs.size(); k++) {
+      const mks_ratfunc &f = fn(fs[k], tag);
+      ns.push_back(f.order);
+      for (int j = 0; j < f.order; j++) {
+        offs.push_back(f.pole[j + 1]);
+        psim.push_back(x_of(x0[k] + j));
+        MKS_CUDA(cudaMemsetAsync(psim.back(), 0, vsz() * sizeof(double), ctx().stream));
+      }
+    }
+    mks_invert_arg arg;
+    arg.max = p->pf[fs[0]].max_cg;
+    arg.nrestart = p->nrestart > 0 ? p->nrestart : 5;
+    arg.parity = MKS_EVEN;
+    arg.prec = prec(tag);
+    arg.resid = resid(fs[0], tag);
+    arg.relresid = 0.0;
+    arg.delta = 0.1;
+    std::vector<mks_invert_result> res(offs.size());
+    const double t0 = wall();
+    const int it = mks_ks_multicg_offset_multi_dev((int)fs.size(), srcs.data(), ns.data(), offs.data(), psim.data(),
+                                                   inaik[fs[0]], &arg, res.data());
+    r->t_solve += wall() - t0;
+    if (it < 0) return it;
+    for (const mks_invert_result &q : res)
+      if (!q.converged) r->unconverged++;
+    r->cg_iters += it;
+    r->n_solves += (int)fs.size();
+    return MKS_OK;
+  }
+
   // out = res_0 src + sum_j res_{j+1} psim_j on even sites
   int rateval(const double *src, int ipf, int tag, int x0, double *out) {
     const mks_ratfunc &f = fn(ipf, tag);
@@ -101,15 +158,31 @@ struct Traj {
     return lincomb_aos_dev(0, src, x.data(), f.res, f.order, out);
   }
 
+  // grsource_rhmc.c: the Gaussians of all fields are drawn first, in field
+  // order (the solves use no random numbers, so the sequence is MILC's)
   int grsource() {
     Context &c = ctx();
     for (int ipf = 0; ipf < p->n_pseudo; ipf++) {
-      MKS_CUDA(cudaMemsetAsync(tmp, 0, vsz() * sizeof(double), c.stream));
-      MKS_TRY(gauss_vec_dev(MKS_EVEN, tmp));
-      if (ipf < MKS_RHMC_MAX_PSEUDO) MKS_TRY(norm2_aos_dev(tmp, 0, &r->grsource_sum[ipf]));
-      MKS_TRY(ratinv(tmp, ipf, 1, 0));
-      MKS_CUDA(cudaMemsetAsync(phi_of(ipf), 0, vsz() * sizeof(double), c.stream));
-      MKS_TRY(rateval(tmp, ipf, 1, 0, phi_of(ipf)));
+      double *g = gtmp + (size_t)ipf * vsz();
+      MKS_CUDA(cudaMemsetAsync(g, 0, vsz() * sizeof(double), c.stream));
+      MKS_TRY(gauss_vec_dev(MKS_EVEN, g));
+      if (ipf < MKS_RHMC_MAX_PSEUDO) MKS_TRY(norm2_aos_dev(g, 0, &r->grsource_sum[ipf]));
+    }
+    for (int gi = 0; gi < (int)eps_distinct.size(); gi++) {
+      const std::vector<int> fs = group(gi);
+      std::vector<const double *> srcs;
+      std::vector<int> x0;
+      int off = 0;
+      for (int f : fs) {
+        srcs.push_back(gtmp + (size_t)f * vsz());
+        x0.push_back(off);
+        off += fn(f, 1).order;
+      }
+      MKS_TRY(ratinv_many(fs, 1, srcs, x0));
+      for (size_t k = 0; k < fs.size(); k++) {
+        MKS_CUDA(cudaMemsetAsync(phi_of(fs[k]), 0, vsz() * sizeof(double), c.stream));
+        MKS_TRY(rateval(srcs[k], fs[k], 1, x0[k], phi_of(fs[k])));
+      }
     }
     return MKS_OK;
   }
@@ -117,14 +190,25 @@ struct Traj {
   int action(double *g, double *h, double *f) {
     MKS_TRY(gauge_action_dev(p->beta, p->u0, p->nflavors, g));
     MKS_TRY(mom_action_dev(h));
-    *f = 0.0;
-    for (int ipf = 0; ipf < p->n_pseudo; ipf++) {
-      MKS_TRY(ratinv(phi_of(ipf), ipf, 2, 0));
-      MKS_TRY(rateval(phi_of(ipf), ipf, 2, 0, tmp));
-      double s;
-      MKS_TRY(norm2_aos_dev(tmp, 0, &s));
-      *f += s;
+    std::vector<double> sf(p->n_pseudo, 0.0);
+    for (int gi = 0; gi < (int)eps_distinct.size(); gi++) {
+      const std::vector<int> fs = group(gi);
+      std::vector<const double *> srcs;
+      std::vector<int> x0;
+      int off = 0;
+      for (int fi : fs) {
+        srcs.push_back(phi_of(fi));
+        x0.push_back(off);
+        off += fn(fi, 2).order;
+      }
+      MKS_TRY(ratinv_many(fs, 2, srcs, x0));
+      for (size_t k = 0; k < fs.size(); k++) {
+        MKS_TRY(rateval(phi_of(fs[k]), fs[k], 2, x0[k], tmp));
+        MKS_TRY(norm2_aos_dev(tmp, 0, &sf[fs[k]]));
+      }
     }
+    *f = 0.0;
+    for (int ipf = 0; ipf < p->n_pseudo; ipf++) *f += sf[ipf];   // field order
     return MKS_OK;
   }
 
@@ -148,11 +232,19 @@ struct Traj {
     std::vector<int> orders(n_naiks, 0);
     std::vector<double> allres;
     int t = 0;
-    for (int g = 0; g < n_naiks; g++)
-      for (int ipf = 0; ipf < p->n_pseudo; ipf++) {
-        if (inaik[ipf] != g) continue;
+    for (int g = 0; g < n_naiks; g++) {
+      const std::vector<int> fs = group(g);
+      std::vector<const double *> srcs;
+      std::vector<int> x0;
+      int off = t;
+      for (int ipf : fs) {
+        srcs.push_back(phi_of(ipf));
+        x0.push_back(off);
+        off += fn(ipf, 0).order;
+      }
+      MKS_TRY(ratinv_many(fs, 0, srcs, x0));
+      for (int ipf : fs) {
         const mks_ratfunc &f = fn(ipf, 0);
-        MKS_TRY(ratinv(phi_of(ipf), ipf, 0, t));
         for (int j = 0; j < f.order; j++) {
           MKS_TRY(mks_dslash_fn_field_dev(x_of(t + j), x_of(t + j), MKS_ODD, g));
           allres.push_back(f.res[j + 1]);
@@ -160,6 +252,7 @@ struct Traj {
         orders[g] += f.order;
         t += f.order;
       }
+    }
     const double t0 = wall();
     std::vector<double2 *> xp(t);
     for (int j = 0; j < t; j++) {
@@ -299,7 +392,7 @@ int mks_rhmc_trajectory(const mks_rhmc_params *p, mks_rhmc_result *r) {
   Traj T;
   T.p = p;
   T.r = r;
-  int total = 0, maxo = 0;
+  int total = 0, maxo = 0, total_gr = 0, total_fa = 0;
   for (int i = 0; i < p->n_pseudo; i++) {
     const mks_pseudofermion &f = p->pf[i];
     const mks_ratfunc *fs[3] = {&f.md, &f.gr, &f.fa};
@@ -311,6 +404,8 @@ int mks_rhmc_trajectory(const mks_rhmc_params *p, mks_rhmc_result *r) {
     }
     if (f.max_cg < 1 || !(f.resid_md > 0) || !(f.resid_fa > 0) || !(f.resid_gr > 0)) return MKS_ERR_ARG;
     total += f.md.order;
+    total_gr += f.gr.order;
+    total_fa += f.fa.order;
     int g = -1;
     for (size_t k = 0; k < T.eps_distinct.size(); k++)
       if (T.eps_distinct[k] == f.naik_eps) g = (int)k;
@@ -324,6 +419,8 @@ int mks_rhmc_trajectory(const mks_rhmc_params *p, mks_rhmc_result *r) {
   if (T.eps_distinct[0] != 0.0) return MKS_ERR_ARG;  // MILC: the first Naik group has epsilon 0
   if (total > 64) return MKS_ERR_ARG;               // force terms per call
   T.max_terms = total > maxo ? total : maxo;
+  T.max_terms = total_gr > T.max_terms ? total_gr : T.max_terms;   // a Naik group's fields solved together
+  T.max_terms = total_fa > T.max_terms ? total_fa : T.max_terms;
   const size_t vb = c.V * 6 * sizeof(double);
   const size_t phi_bytes = (size_t)p->n_pseudo * vb;
   if (!p->refresh && (!g_phi || g_phi_bytes != phi_bytes)) return MKS_ERR_STATE;
@@ -335,10 +432,12 @@ int mks_rhmc_trajectory(const mks_rhmc_params *p, mks_rhmc_result *r) {
   T.phi = g_phi;
   int rc = dev_alloc((void **)&T.xs, (size_t)T.max_terms * vb);
   if (rc >= 0) rc = dev_alloc((void **)&T.tmp, vb);
+  if (rc >= 0) rc = dev_alloc((void **)&T.gtmp, (size_t)p->n_pseudo * vb);
   if (rc >= 0) rc = dev_alloc((void **)&T.xs_soa, (size_t)total * 6 * c.Vh * sizeof(double2));
   if (rc >= 0) rc = T.run();
   dev_free(T.xs);
   dev_free(T.tmp);
+  dev_free(T.gtmp);
   dev_free(T.xs_soa);
   return rc;
 }

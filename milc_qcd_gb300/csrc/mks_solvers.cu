@@ -1544,11 +1544,8 @@ struct MsState {
   int retired[MAXSH];
 };
 
-struct FinMsAlpha {
-  MsState *st;
-  __device__ void operator()(const double *t, int) const {
-    if (threadIdx.x != 0) return;
-    MsState &m = *st;
+// the zeta / beta / alpha recurrences of one field after K2 (t: its three sums)
+__device__ __forceinline__ void ms_alpha(MsState &m, const double *t) {
     if (m.status != ST_RUN) return;
     if (m.need_scroll) {
       for (int j = 0; j < m.num_now; j++) {
@@ -1591,17 +1588,21 @@ struct FinMsAlpha {
         m.alpha[j] = 0.0;
     }
     if (!isfinite(m.beta_i[jl])) m.status = ST_HOST;
+}
+
+struct FinMsAlpha {
+  MsState *st;
+  __device__ void operator()(const double *t, int) const {
+    if (threadIdx.x != 0) return;
+    ms_alpha(*st, t);
   }
 };
 
-struct FinMsUpdate {
-  MsState *st;
-  int *skip;
-  __device__ void operator()(const double *t, int) const {
-    if (threadIdx.x != 0) return;
-    MsState &m = *st;
+// the state of one field after K3 (rsq: the new |r|^2): retirement of
+// converged shifts, stop, reliable-update request
+__device__ __forceinline__ void ms_update(MsState &m, double rsq) {
     if (m.status == ST_RUN) {
-      m.rsq = t[0];
+      m.rsq = rsq;
       m.need_scroll = 1;
       if (m.rsqretire > 0)
         for (int j = 0; j < m.num_now; j++)
@@ -1616,20 +1617,52 @@ struct FinMsUpdate {
         if (rn < m.delta * m.maxrr) { m.status = ST_HOST; m.want_reliable = 1; }
       }
     }
-    *skip = (m.status != ST_RUN);
+}
+
+struct FinMsUpdate {
+  MsState *st;
+  int *skip;
+  __device__ void operator()(const double *t, int) const {
+    if (threadIdx.x != 0) return;
+    ms_update(*st, t[0]);
+    *skip = (st->status != ST_RUN);
   }
 };
 
-template <typename R> struct OpShiftUpdate {
-  typedef typename VT<R>::v2 T2;
-  T2 *psim[MAXSH], *pm[MAXSH];
-  T2 *r, *ttt, *cgp;
-  __half2 *p16;
-  float *p16n;
-  const MsState *st;
-  int Vh;
-  __device__ void operator()(int h, int, double *out) const {
-    const MsState &m = *st;
+// several fields in one multi-shift (one per row k, field map[k])
+constexpr int MSF = 4;
+struct FinMsAlphaM {
+  MsState *st;
+  int map[MSF];
+  __device__ void operator()(const double *t, int n) const {
+    const int k = threadIdx.x;
+    if (k < n) ms_alpha(st[map[k]], t + 3 * k);
+  }
+};
+struct FinMsUpdateM {
+  MsState *st;
+  int *skip;
+  int map[MSF];
+  __device__ void operator()(const double *t, int n) const {
+    const int k = threadIdx.x;
+    if (k < n) ms_update(st[map[k]], t[k]);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int any = 0;
+      for (int i = 0; i < n; i++) any |= (st[map[i]].status != ST_RUN);
+      *skip = any;
+    }
+  }
+};
+
+// K3 at one site for one field: r += beta ttt, every shift's psim and pm,
+// the lowest shift's p (and its FP16 shadow); out[0] = |r|^2 at the site
+template <typename R>
+__device__ __forceinline__ void ms_site_update(const MsState &m, typename VT<R>::v2 *const *psim,
+                                               typename VT<R>::v2 *const *pm, typename VT<R>::v2 *r,
+                                               const typename VT<R>::v2 *ttt, typename VT<R>::v2 *cgp,
+                                               __half2 *p16, float *p16n, int h, int Vh, double *out) {
+    typedef typename VT<R>::v2 T2;
     const int n = m.num_now, jl = m.j_low;
     const R bl = (R)m.beta_i[jl];
     T2 rn[3];
@@ -1673,6 +1706,32 @@ template <typename R> struct OpShiftUpdate {
       }
     }
     out[0] = rr;
+}
+
+template <typename R> struct OpShiftUpdate {
+  typedef typename VT<R>::v2 T2;
+  T2 *psim[MAXSH], *pm[MAXSH];
+  T2 *r, *ttt, *cgp;
+  __half2 *p16;
+  float *p16n;
+  const MsState *st;
+  int Vh;
+  __device__ void operator()(int h, int, double *out) const {
+    ms_site_update<R>(*st, psim, pm, r, ttt, cgp, p16, p16n, h, Vh, out);
+  }
+};
+
+// the same for several fields, one per row k (field map[k])
+template <typename R> struct OpShiftUpdateM {
+  typedef typename VT<R>::v2 T2;
+  T2 *psim[MSF][MAXSH], *pm[MSF][MAXSH];
+  T2 *r[MSF], *ttt[MSF], *cgp[MSF];
+  const MsState *st;
+  int map[MSF];
+  int Vh;
+  __device__ void operator()(int h, int k, double *out) const {
+    const int f = map[k];
+    ms_site_update<R>(st[f], psim[f], pm[f], r[f], ttt[f], cgp[f], nullptr, nullptr, h, Vh, out);
   }
 };
 
@@ -1941,6 +2000,232 @@ static int multishift_core(const LinkSlot &sl, int par, int prec, const double2 
   return MKS_OK;
 }
 
+// Several fields (sources), each with its own offsets, advanced together
+// on the same links: one multi-source D_eo pair per iteration reads the
+// links once for all running fields, and one update launch advances every
+// field's shifts.  FP32 sloppy vectors with FP64 reliable updates of each
+// field's lowest shift, exactly as multishift_core does for one field; a
+// field that stops leaves the launches (the kernels are rebuilt for the
+// remaining fields).  On exit x64[f][j] holds every field's solutions.
+static int multishift_multi_core(const LinkSlot &sl, int par, int nf, const double2 *const *src64, const int *nsh,
+                                 const double *const *offsets, double resid, int niter, double2 *const *const *x64,
+                                 double delta, MsState *hs) {
+  typedef float2 T2;
+  Context &c = ctx();
+  const int Vh = (int)c.Vh;
+  const size_t n = 3 * c.Vh;
+  T2 *r[MSF], *cgp[MSF], *ttt[MSF], *t[MSF], *pm[MSF][MAXSH], *psim[MSF][MAXSH];
+  for (int f = 0; f < nf; f++) {
+    const std::string k = std::to_string(f);
+    MKS_TRY(wsv("msm_r_" + k, n, &r[f]));
+    MKS_TRY(wsv("msm_p_" + k, n, &cgp[f]));
+    MKS_TRY(wsv("msm_ttt_" + k, n, &ttt[f]));
+    MKS_TRY(wsv("msm_t_" + k, n, &t[f]));
+    for (int j = 0; j < nsh[f]; j++) {
+      MKS_TRY(wsv("msm_pm_" + k + "_" + std::to_string(j), n, &pm[f][j]));
+      MKS_TRY(wsv("msm_x_" + k + "_" + std::to_string(j), n, &psim[f][j]));
+    }
+  }
+  MsState *st;
+  int *skip;
+  double *tot, *tot1;
+  MKS_TRY(wsv("msm_state", MSF, &st));
+  MKS_TRY(wsv("msm_skip", 1, &skip));
+  MKS_TRY(wsv("msm_tot", 3 * MSF, &tot));
+  MKS_TRY(wsv("msm_tot1", 4, &tot1));
+  // initial state of every field (ks_multicg_offset.c:180-262)
+  for (int f = 0; f < nf; f++) {
+    MsState &h = hs[f];
+    memset(&h, 0, sizeof h);
+    double offset_low = 1.0e20;
+    int j_low = 0;
+    for (int j = 0; j < nsh[f]; j++) {
+      h.shifts[j] = offsets[f][j];
+      if (offsets[f][j] < offset_low) { offset_low = offsets[f][j]; j_low = j; }
+    }
+    for (int j = 0; j < nsh[f]; j++)
+      if (j != j_low) h.shifts[j] -= h.shifts[j_low];
+    h.shift0 = -h.shifts[j_low];
+    h.j_low = j_low; h.num_now = nsh[f]; h.num_offsets = nsh[f]; h.niter = niter;
+    for (int j = 0; j < nsh[f]; j++) { h.zeta_im1[j] = h.zeta_i[j] = 1.0; h.beta_im1[j] = -1.0; h.alpha[j] = 0.0; }
+    OpShiftInit<float> op;
+    memset(&op, 0, sizeof op);
+    for (int j = 0; j < nsh[f]; j++) { op.psim[j] = psim[f][j]; op.pm[j] = pm[f][j]; }
+    op.r = r[f]; op.cgp = cgp[f]; op.src = src64[f]; op.Vh = Vh; op.n = nsh[f];
+    MKS_TRY((launch_site<OpShiftInit<float>, 1, FinNone>(MKS_K_SHIFT, op, FinNone(), nullptr, 1, tot1)));
+    double sn = 0;
+    MKS_CUDA(cudaMemcpyAsync(&sn, tot1, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    MKS_CUDA(cudaStreamSynchronize(c.stream));
+    h.source_norm = sn;
+    h.rsq = sn;
+    h.rsqstop = resid * resid * sn;
+    h.iter = 1;
+    h.status = sn == 0.0 ? ST_DONE : ST_RUN;
+    h.maxrr = sqrt(sn);
+    h.delta = delta;
+    h.rsqretire = 0.01 * h.rsqstop;
+    for (int j = 0; j < nsh[f]; j++) MKS_CUDA(cudaMemsetAsync(x64[f][j], 0, n * sizeof(double2), c.stream));
+  }
+  MKS_CUDA(cudaMemcpyAsync(st, hs, nf * sizeof(MsState), cudaMemcpyHostToDevice, c.stream));
+  const int zero = 0;
+  MKS_CUDA(cudaMemcpyAsync(skip, &zero, sizeof zero, cudaMemcpyHostToDevice, c.stream));
+  const int np = poll_interval();
+  LinkSet32 L = links32(sl);
+  int guard = 0;
+  while (true) {
+    int act[MSF], nact = 0;
+    for (int f = 0; f < nf; f++)
+      if (hs[f].status == ST_RUN) act[nact++] = f;
+    if (nact == 0) break;
+    auto issue = [&]() -> int {
+      for (int k = 0; k < np; k++) {
+        DslashArgs<VecF32, VecF32, VecF32> a1;
+        memset(&a1, 0, sizeof a1);
+        a1.out_par = 1 - par; a1.nsrc = nact; a1.skip = skip;
+        for (int q = 0; q < nact; q++) { a1.in[q].p = cgp[act[q]]; a1.out[q].p = t[act[q]]; }
+        MKS_TRY((launch_dslash<float, LinkF32, VecF32, VecF32, EPI_PLAIN, 0>(MKS_K_DSLASH_F32, L.fat, L.lng, a1,
+                                                                           FinNone())));
+        DslashArgs<VecF32, VecF32, VecF32> a2;
+        memset(&a2, 0, sizeof a2);
+        a2.out_par = par; a2.nsrc = nact; a2.skip = skip; a2.totals = tot;
+        FinMsAlphaM fa;
+        fa.st = st;
+        for (int q = 0; q < nact; q++) {
+          const int f = act[q];
+          a2.in[q].p = t[f]; a2.out[q].p = ttt[f]; a2.p[q].p = cgp[f]; a2.r[q].p = r[f]; a2.coef[q] = hs[f].shift0;
+          fa.map[q] = f;
+        }
+        MKS_TRY((launch_dslash<float, LinkF32, VecF32, VecF32, EPI_AXPY, 3>(MKS_K_DSLASH_F32, L.fat, L.lng, a2, fa)));
+        OpShiftUpdateM<float> up;
+        memset(&up, 0, sizeof up);
+        FinMsUpdateM fu;
+        fu.st = st; fu.skip = skip;
+        for (int f = 0; f < nf; f++) {
+          for (int j = 0; j < nsh[f]; j++) { up.psim[f][j] = psim[f][j]; up.pm[f][j] = pm[f][j]; }
+          up.r[f] = r[f]; up.ttt[f] = ttt[f]; up.cgp[f] = cgp[f];
+        }
+        for (int q = 0; q < nact; q++) { up.map[q] = act[q]; fu.map[q] = act[q]; }
+        up.st = st; up.Vh = Vh;
+        MKS_TRY((launch_site<OpShiftUpdateM<float>, 1, FinMsUpdateM>(MKS_K_SHIFT, up, fu, skip, nact)));
+      }
+      return MKS_OK;
+    };
+    std::vector<uint64_t> key;
+    key_push(key, -2); key_push(key, par); key_push(key, np); key_push(key, (int)c.timing);
+    key_push(key, c.geom.Vh); key_push(key, c.geom.nx); key_push(key, c.geom.ny); key_push(key, c.geom.nz);
+    key_push(key, c.geom.nt); key_push(key, sl.fat32a); key_push(key, sl.lng32a); key_push(key, sl.fat32b);
+    key_push(key, sl.lng32b); key_push(key, st); key_push(key, skip); key_push(key, tot);
+    key_push(key, c.red.partials); key_push(key, c.red.count); key_push(key, nact);
+    for (int q = 0; q < nact; q++) {
+      const int f = act[q];
+      key_push(key, f); key_push(key, hs[f].shift0); key_push(key, nsh[f]); key_push(key, r[f]);
+      key_push(key, cgp[f]); key_push(key, ttt[f]); key_push(key, t[f]);
+    }
+    for (int f = 0; f < nf; f++)
+      for (int j = 0; j < nsh[f]; j++) { key_push(key, psim[f][j]); key_push(key, pm[f][j]); }
+    // poll until a field needs the host, then serve it
+    bool host = false;
+    while (!host) {
+      MKS_TRY(graph_batch(key, issue));
+      MKS_CUDA(cudaMemcpyAsync(hs, st, nf * sizeof(MsState), cudaMemcpyDeviceToHost, c.stream));
+      MKS_CUDA(cudaStreamSynchronize(c.stream));
+      MKS_TRY(red_check());
+      if (++guard > 10000000) return MKS_ERR_TIMEOUT;
+      for (int q = 0; q < nact; q++) host |= hs[act[q]].status != ST_RUN;
+    }
+    for (int q = 0; q < nact; q++) {
+      const int f = act[q];
+      MsState &h = hs[f];
+      if (h.status != ST_HOST || !h.want_reliable) continue;   // stopped fields leave the launches
+      // reliable update of field f: fold, FP64 residual of its lowest shift
+      MKS_TRY(ms_fold(nsh[f], x64[f], (void *const *)psim[f]));
+      double2 *t64, *dd64;
+      MKS_TRY(wsv("ms_rel_t64", n, &t64));
+      MKS_TRY(wsv("ms_rel_dd64", n, &dd64));
+      double2 *xl = x64[f][h.j_low];
+      MKS_TRY(apply_DD64(sl, par, 1, &xl, &t64, &dd64));
+      OpMsResid op;
+      op.src = src64[f]; op.ddx = dd64; op.x = xl; op.r32 = r[f]; op.sigma = offsets[f][h.j_low]; op.Vh = Vh;
+      MKS_TRY((launch_site<OpMsResid, 1, FinNone>(MKS_K_SHIFT, op, FinNone(), nullptr, 1, tot1)));
+      double rr = 0;
+      MKS_CUDA(cudaMemcpyAsync(&rr, tot1, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+      MKS_CUDA(cudaStreamSynchronize(c.stream));
+      h.rsq = rr;
+      h.maxrr = sqrt(rr);
+      h.want_reliable = 0;
+      h.n_reliable++;
+      h.status = (h.rsq <= h.rsqstop || !std::isfinite(h.rsq)) ? ST_HOST : ST_RUN;
+    }
+    MKS_CUDA(cudaMemcpyAsync(st, hs, nf * sizeof(MsState), cudaMemcpyHostToDevice, c.stream));
+    MKS_CUDA(cudaMemcpyAsync(skip, &zero, sizeof zero, cudaMemcpyHostToDevice, c.stream));
+  }
+  for (int f = 0; f < nf; f++) MKS_TRY(ms_fold(nsh[f], x64[f], (void *const *)psim[f]));
+  MKS_CUDA(cudaStreamSynchronize(c.stream));
+  return MKS_OK;
+}
+
+// nf fields on one slot: offsets, psim_dev and res are the fields' lists one
+// after the other (num_offsets[f] entries each)
+static int multishift_multi_dev(int nf, const double *const *src_dev, const int *num_offsets, const double *offsets,
+                                double *const *psim_dev, int slot, const mks_invert_arg *arg, mks_invert_result *res) {
+  Context &c = ctx();
+  const LinkSlot &sl = c.slots[slot];
+  int par;
+  MKS_TRY(parity_index(arg->parity, &par));
+  const double2 *src64[MSF];
+  const double *offs[MSF];
+  double2 *x64s[MSF][MAXSH];
+  double2 *const *x64p[MSF];
+  int base[MSF + 1];
+  base[0] = 0;
+  for (int f = 0; f < nf; f++) {
+    base[f + 1] = base[f] + num_offsets[f];
+    offs[f] = offsets + base[f];
+    for (int j = 0; j < num_offsets[f]; j++)
+      if (!(offs[f][j] > 0)) return MKS_ERR_ARG;
+    double2 *s64;
+    MKS_TRY(wsv("msm_src64_" + std::to_string(f), 3 * c.Vh, &s64));
+    MKS_TRY(vec_aos_to_soa64(src_dev[f], s64, par));
+    src64[f] = s64;
+    for (int j = 0; j < num_offsets[f]; j++)
+      MKS_TRY(wsv("msm_x64_" + std::to_string(f) + "_" + std::to_string(j), 3 * c.Vh, &x64s[f][j]));
+    x64p[f] = x64s[f];
+  }
+  MsState hs[MSF];
+  MKS_TRY(multishift_multi_core(sl, par, nf, src64, num_offsets, offs, arg->resid, arg->max * arg->nrestart, x64p,
+                                arg->delta > 0 ? arg->delta : 0.1, hs));
+  // FP64 check of every shift of every field, refinement of those that miss
+  // (ks_multicg.c:170-228), blocks of up to MAXSRC shifts across the fields
+  const int total = base[nf];
+  std::vector<int> fld(total), shf(total);
+  for (int f = 0; f < nf; f++)
+    for (int j = 0; j < num_offsets[f]; j++) { fld[base[f] + j] = f; shf[base[f] + j] = j; }
+  for (int b0 = 0; b0 < total; b0 += MAXSRC) {
+    const int nb = total - b0 < MAXSRC ? total - b0 : MAXSRC;
+    CgFields cf;
+    memset(&cf, 0, sizeof cf);
+    MKS_TRY(alloc_cg_fields(cf, nb, arg->prec));
+    double sig[MAXSRC];
+    for (int q = 0; q < nb; q++) {
+      const int f = fld[b0 + q], j = shf[b0 + q];
+      cf.src[q] = (double2 *)src64[f];
+      cf.x[q] = x64s[f][j];
+      sig[q] = offs[f][j];
+    }
+    MKS_TRY(block_cg_shifted(slot, par, nb, sig, arg, cf, res + b0));
+    for (int q = 0; q < nb; q++) {
+      const int f = fld[b0 + q];
+      MKS_TRY(vec_soa64_to_aos(cf.x[q], psim_dev[b0 + q], par));
+      res[b0 + q].final_iters += hs[f].iter;
+      res[b0 + q].reliable_updates += hs[f].n_reliable;
+    }
+  }
+  MKS_CUDA(cudaStreamSynchronize(c.stream));
+  int mx = 0;
+  for (int q = 0; q < total; q++) mx = res[q].final_iters > mx ? res[q].final_iters : mx;
+  return mx;
+}
+
 static int multishift_dev(const double *src_dev, double *const *psim_dev, const double *offsets, int nsh, int slot,
                           const mks_invert_arg *arg, mks_invert_result *res) {
   Context &c = ctx();
@@ -2016,6 +2301,33 @@ int mks_ks_multicg_offset_field_dev(const double *src_dev, double *const *psim_d
   if (num_offsets == 0) return 0;
   if (num_offsets < 0 || num_offsets > MAXSH || !src_dev || !psim_dev || !offsets || !res) return MKS_ERR_ARG;
   return multishift_dev(src_dev, psim_dev, offsets, num_offsets, slot, arg, res);
+}
+
+int mks_ks_multicg_offset_multi_dev(int nf, const double *const *src_dev, const int *num_offsets,
+                                    const double *offsets, double *const *psim_dev, int slot,
+                                    const mks_invert_arg *arg, mks_invert_result *res) {
+  MKS_TRY(check_ready());
+  MKS_TRY(slot_ok(slot));
+  MKS_TRY(check_arg(arg, true));
+  if (nf < 1 || nf > MSF || !src_dev || !num_offsets || !offsets || !psim_dev || !res) return MKS_ERR_ARG;
+  int total = 0;
+  for (int f = 0; f < nf; f++) {
+    if (num_offsets[f] < 1 || num_offsets[f] > MAXSH || !src_dev[f]) return MKS_ERR_ARG;
+    total += num_offsets[f];
+  }
+  if (arg->prec != MKS_PREC_SINGLE || nf == 1) {
+    // one field at a time (FP64 keeps MILC's single-field semantics)
+    int mx = 0, off = 0;
+    for (int f = 0; f < nf; f++) {
+      const int it = multishift_dev(src_dev[f], psim_dev + off, offsets + off, num_offsets[f], slot, arg, res + off);
+      if (it < 0) return it;
+      mx = it > mx ? it : mx;
+      off += num_offsets[f];
+    }
+    return mx;
+  }
+  (void)total;
+  return multishift_multi_dev(nf, src_dev, num_offsets, offsets, psim_dev, slot, arg, res);
 }
 
 int mks_ks_multicg_offset_field(const double *src, double *const *psim, const double *offsets, int num_offsets,
