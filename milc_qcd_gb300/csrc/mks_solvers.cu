@@ -1227,22 +1227,27 @@ static int congrad_block_dev(int nsrc, const double *const *src_dev, double *con
   return MKS_OK;
 }
 
-// host arrays: copy in, solve in batches of MAXSRC, copy out
+// host arrays: copy in, solve in batches of MAXSRC, copy out.  A parity
+// solve reads and writes only the sites of its parity, which are one
+// contiguous half of MILC's even-first field: only that half moves.
 static int congrad_block_host(int nsrc, const double *const *src, double *const *dst, double mass, int slot,
                               const mks_invert_arg *arg, mks_invert_result *res) {
   Context &c = ctx();
-  size_t bytes = c.V * 6 * sizeof(double);
+  int par;
+  MKS_TRY(parity_index(arg->parity, &par));
+  const size_t off = (size_t)par * c.Vh * 6, bytes = c.Vh * 6 * sizeof(double);
   for (int b0 = 0; b0 < nsrc; b0 += MAXSRC) {
     int nb = nsrc - b0 < MAXSRC ? nsrc - b0 : MAXSRC;
     double *ds[MAXSRC], *dd[MAXSRC];
     for (int s = 0; s < nb; s++) {
       MKS_TRY(wsv("hsrc" + std::to_string(s), 6 * c.V, &ds[s]));
       MKS_TRY(wsv("hdst" + std::to_string(s), 6 * c.V, &dd[s]));
-      MKS_CUDA(cudaMemcpyAsync(ds[s], src[b0 + s], bytes, cudaMemcpyHostToDevice, c.stream));
-      MKS_CUDA(cudaMemcpyAsync(dd[s], dst[b0 + s], bytes, cudaMemcpyHostToDevice, c.stream));
+      MKS_CUDA(cudaMemcpyAsync(ds[s] + off, src[b0 + s] + off, bytes, cudaMemcpyHostToDevice, c.stream));
+      MKS_CUDA(cudaMemcpyAsync(dd[s] + off, dst[b0 + s] + off, bytes, cudaMemcpyHostToDevice, c.stream));
     }
     MKS_TRY(congrad_block_dev(nb, ds, dd, mass, slot, arg, res + b0));
-    for (int s = 0; s < nb; s++) MKS_CUDA(cudaMemcpyAsync(dst[b0 + s], dd[s], bytes, cudaMemcpyDeviceToHost, c.stream));
+    for (int s = 0; s < nb; s++)
+      MKS_CUDA(cudaMemcpyAsync(dst[b0 + s] + off, dd[s] + off, bytes, cudaMemcpyDeviceToHost, c.stream));
     MKS_CUDA(cudaStreamSynchronize(c.stream));
   }
   return MKS_OK;
@@ -2338,19 +2343,20 @@ int mks_ks_multicg_offset_field(const double *src, double *const *psim, const do
   if (num_offsets == 0) return 0;
   if (num_offsets < 0 || num_offsets > MAXSH || !src || !psim || !offsets || !res) return MKS_ERR_ARG;
   Context &c = ctx();
-  size_t bytes = c.V * 6 * sizeof(double);
+  // the solve reads the source and writes the solutions on arg->parity only
+  // (one contiguous half of MILC's even-first fields); psim is output only
+  int par;
+  MKS_TRY(parity_index(arg->parity, &par));
+  const size_t off = (size_t)par * c.Vh * 6, bytes = c.Vh * 6 * sizeof(double);
   double *ds;
   double *dp[MAXSH];
   MKS_TRY(wsv("hsrc0", 6 * c.V, &ds));
-  MKS_CUDA(cudaMemcpyAsync(ds, src, bytes, cudaMemcpyHostToDevice, c.stream));
-  for (int j = 0; j < num_offsets; j++) {
-    MKS_TRY(wsv("hpsim" + std::to_string(j), 6 * c.V, &dp[j]));
-    MKS_CUDA(cudaMemcpyAsync(dp[j], psim[j], bytes, cudaMemcpyHostToDevice, c.stream));
-  }
+  MKS_CUDA(cudaMemcpyAsync(ds + off, src + off, bytes, cudaMemcpyHostToDevice, c.stream));
+  for (int j = 0; j < num_offsets; j++) MKS_TRY(wsv("hpsim" + std::to_string(j), 6 * c.V, &dp[j]));
   int it = multishift_dev(ds, dp, offsets, num_offsets, slot, arg, res);
   if (it < 0) return it;
   for (int j = 0; j < num_offsets; j++)
-    MKS_CUDA(cudaMemcpyAsync(psim[j], dp[j], bytes, cudaMemcpyDeviceToHost, c.stream));
+    MKS_CUDA(cudaMemcpyAsync(psim[j] + off, dp[j] + off, bytes, cudaMemcpyDeviceToHost, c.stream));
   MKS_CUDA(cudaStreamSynchronize(c.stream));
   return it;
 }
