@@ -284,20 +284,20 @@ __device__ __forceinline__ M3<R> mul_na(const M3<R> &a, const M3<R> &b) {  // a 
 template <typename R>
 __device__ __forceinline__ M3<R> walk_r(const Geom &g, const double2 *U, int c[4], const signed char *path, int len) {
   const int L[4] = {g.nx, g.ny, g.nz, g.nt};
+  // the product starts from the first link itself (the identity product it
+  // replaces is exact, so the result is the same to the last bit)
   M3<R> P;
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) P.e[i][j] = {i == j ? (R)1 : (R)0, (R)0};
   for (int k = 0; k < len; k++) {
     const int d = path[k];
     if (d < 4) {
-      P = mul_nn<R>(P, to_r<R>(load_link(g, U, c, d, true)));
+      const M3<R> Lk = to_r<R>(load_link(g, U, c, d, true));
+      P = k ? mul_nn<R>(P, Lk) : Lk;
       c[d] = wrap_add(c[d], 1, L[d]);
     } else {
       const int dd = 7 - d;
       c[dd] = wrap_add(c[dd], -1, L[dd]);
-      P = mul_na<R>(P, to_r<R>(load_link(g, U, c, dd, true)));
+      const M3<R> Lk = to_r<R>(load_link(g, U, c, dd, true));
+      P = k ? mul_na<R>(P, Lk) : tadj<R>(Lk);
     }
   }
   return P;
@@ -312,19 +312,17 @@ __device__ __forceinline__ M3<float> walk32(const Geom &g, const float2 *U32, in
                                             int len) {
   const int L[4] = {g.nx, g.ny, g.nz, g.nt};
   M3<float> P;
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) P.e[i][j] = {i == j ? 1.f : 0.f, 0.f};
   for (int k = 0; k < len; k++) {
     const int d = path[k];
     if (d < 4) {
-      P = mul_nn<float>(P, load_link32(g, U32, c, d));
+      const M3<float> Lk = load_link32(g, U32, c, d);
+      P = k ? mul_nn<float>(P, Lk) : Lk;
       c[d] = wrap_add(c[d], 1, L[d]);
     } else {
       const int dd = 7 - d;
       c[dd] = wrap_add(c[dd], -1, L[dd]);
-      P = mul_na<float>(P, load_link32(g, U32, c, dd));
+      const M3<float> Lk = load_link32(g, U32, c, dd);
+      P = k ? mul_na<float>(P, Lk) : tadj<float>(Lk);
     }
   }
   return P;
