@@ -241,6 +241,21 @@ int vec_aos_to_soa64(const double *aos_dev, double2 *soa, int par) {
   MKS_CUDA(cudaGetLastError());
   return MKS_OK;
 }
+__global__ void k_vec_aos_to_soa32(const double *__restrict__ aos, float2 *__restrict__ soa, int par, int Vh) {
+  int h = blockIdx.x * blockDim.x + threadIdx.x;
+  if (h >= Vh) return;
+  const double *s = aos + ((size_t)par * Vh + h) * 6;
+#pragma unroll
+  for (int c = 0; c < 3; c++) soa[(size_t)c * Vh + h] = make_float2((float)s[2 * c], (float)s[2 * c + 1]);
+}
+int vec_aos_to_soa32(const double *aos_dev, float2 *soa, int par) {
+  Context &c = g_ctx;
+  int Vh = (int)c.Vh;
+  k_vec_aos_to_soa32<<<grid_for(Vh, 256), 256, 0, c.stream>>>(aos_dev, soa, par, Vh);
+  c.launches++;
+  MKS_CUDA(cudaGetLastError());
+  return MKS_OK;
+}
 int vec_soa64_to_aos(const double2 *soa, double *aos_dev, int par) {
   Context &c = g_ctx;
   int Vh = (int)c.Vh;

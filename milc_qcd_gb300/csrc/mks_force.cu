@@ -481,8 +481,9 @@ struct ForceRun {
     return MKS_OK;
   }
 
+  // xr: the inputs already in precision R (FP32 SoA), else converted from xs
   static int hisq(double eps, const double *residues, double2 *const *xs, int nterms, const int *orders, int n_naiks,
-                  double *mom_dev, double2 *ku_out) {
+                  double *mom_dev, double2 *ku_out, T2 *const *xr = nullptr) {
     Context &c = ctx();
     const size_t Vh = c.Vh, nl = 8 * 9 * Vh, nm = 2 * 9 * Vh;
     const ForceCoeffs c1 = {1.0 / 8.0, 0.0, -1.0 / 16.0, 1.0 / 64.0, -1.0 / 384.0, 0.0};
@@ -491,7 +492,7 @@ struct ForceRun {
     const ForceCoeffs c3 = {1.0 / 8.0, -1.0 / 24.0, 0, 0, 0, 0};
     const bool low = sizeof(R) < 8;
     // Kf Kl KW KV KU, S1 S2 K1 K2, and in FP32 the U and W copies and the inputs
-    const size_t total = 5 * nl + 4 * nm + (low ? 2 * nl + (size_t)nterms * 6 * Vh : 0);
+    const size_t total = 5 * nl + 4 * nm + (low ? 2 * nl + (xr ? 0 : (size_t)nterms * 6 * Vh) : 0);
     T2 *buf = nullptr;
     MKS_TRY(dev_alloc((void **)&buf, total * sizeof(T2)));
     T2 *Kf = buf, *Kl = Kf + nl, *KW = Kl + nl, *KV = KW + nl, *KU = KV + nl;
@@ -508,7 +509,11 @@ struct ForceRun {
       if ((rc = field_r(c.auxW, Wcp, nl, &W)) < 0) break;
       OuterArgs<R> oa;
       memset(&oa, 0, sizeof oa);
-      if ((rc = inputs(xs, nterms, xs32, oa)) < 0) break;
+      if (xr) {
+        for (int j = 0; j < nterms; j++) oa.x[j] = xr[j];
+      } else if ((rc = inputs(xs, nterms, xs32, oa)) < 0) {
+        break;
+      }
       for (int j = 0; j < nterms; j++) oa.res[j] = residues[j];
       // level 2 with every term (the Naik group-0 table covers all terms)
       oa.j0 = 0; oa.j1 = nterms; oa.scale = 1.0;
@@ -590,6 +595,13 @@ int force_dev(double eps, const double *residues, double2 *const *xs, int nterms
   if (ctx().md_prec == MKS_PREC_SINGLE)
     return ForceRun<float>::hisq(eps, residues, xs, nterms, orders, n_naiks, mom_dev, ku_out);
   return ForceRun<double>::hisq(eps, residues, xs, nterms, orders, n_naiks, mom_dev, ku_out);
+}
+
+int force_dev32(double eps, const double *residues, float2 *const *xs32, int nterms, const int *orders,
+                int n_naiks, double *mom_dev) {
+  g_force_flops = 0.0;
+  if (ctx().md_prec != MKS_PREC_SINGLE) return MKS_ERR_STATE;
+  return ForceRun<float>::hisq(eps, residues, nullptr, nterms, orders, n_naiks, mom_dev, nullptr, xs32);
 }
 
 int force_asqtad_dev(double eps, const double *residues, double2 *const *xs, int nterms, double *mom_dev,

@@ -315,6 +315,13 @@ int links_from_aux(int action, int n_naiks, const double *eps_naik, double u0);
 // fermion force on device SoA solution fields (mks_force.cu)
 int force_dev(double eps, const double *residues, double2 *const *xs, int nterms, const int *orders, int n_naiks,
               double *mom_dev, double2 *ku_out);
+// the same in the FP32 molecular-dynamics setting with the solutions already
+// FP32 SoA, full lattice [2][3][Vh] per term
+int force_dev32(double eps, const double *residues, float2 *const *xs32, int nterms, const int *orders,
+                int n_naiks, double *mom_dev);
+// FP32 multi-source D on one parity: out_s (parity out_par) = D in_s (other
+// parity), SoA [3][Vh] fields, slot's FP32 links, any number of sources
+int dslash32_multi(int slot, int out_par, int nsrc, float2 *const *in, float2 *const *out);
 
 // ------------------------------------------------------------------
 // host-side context
@@ -398,6 +405,7 @@ inline int grid_for(size_t n, int block) { return (int)((n + block - 1) / block)
 // layout conversion (mks_context.cu)
 int vec_aos_to_soa64(const double *aos_dev, double2 *soa, int par);   // one parity from a full AoS field
 int vec_soa64_to_aos(const double2 *soa, double *aos_dev, int par);
+int vec_aos_to_soa32(const double *aos_dev, float2 *soa, int par);    // one parity, rounded to FP32
 int links_aos_to_soa64(const double *aos_dev, double2 *soa);          // [V][4][18] -> [2][4][9][Vh]
 int links_soa64_to_aos(const double2 *soa, double *aos_dev);
 int links_make_lowprec(LinkSlot &s);

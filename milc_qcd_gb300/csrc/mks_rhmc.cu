@@ -37,6 +37,7 @@ struct Traj {
   double *xs = nullptr;            // [max_terms][V][6] solutions (AoS)
   double *tmp = nullptr;           // [V][6]
   double *gtmp = nullptr;          // [n_pseudo][V][6] heat-bath Gaussians
+  float2 *xs32 = nullptr;          // [terms][2][3][Vh] force input, FP32 setting
   double2 *xs_soa = nullptr;       // [max_terms][2][3][Vh] force input
   int max_terms = 0;
 
@@ -224,14 +225,19 @@ struct Traj {
   }
 
   // update_h_rhmc.c:40-105: X_j = (M^dag M + pole)^-1 phi on even sites,
-  // D_oe X_j on odd sites, all fields grouped by Naik epsilon, one force call
+  // D_oe X_j on odd sites, all fields grouped by Naik epsilon, one force call.
+  // In the FP32 molecular-dynamics setting the solutions go to FP32 and
+  // D_oe X_j is applied in FP32 (multi-source, the slot's FP32 links) --
+  // the force that consumes them computes in FP32 -- else in FP64 as MILC.
   int update_h_fermion(double eps) {
     Context &c = ctx();
     MKS_TRY(links());
     const int n_naiks = (int)eps_distinct.size();
+    const bool low = c.md_prec == MKS_PREC_SINGLE;
     std::vector<int> orders(n_naiks, 0);
     std::vector<double> allres;
     int t = 0;
+    double t_doe = 0.0;
     for (int g = 0; g < n_naiks; g++) {
       const std::vector<int> fs = group(g);
       std::vector<const double *> srcs;
@@ -243,25 +249,44 @@ struct Traj {
         off += fn(ipf, 0).order;
       }
       MKS_TRY(ratinv_many(fs, 0, srcs, x0));
+      const double td = wall();
+      const int tg = t;
       for (int ipf : fs) {
         const mks_ratfunc &f = fn(ipf, 0);
         for (int j = 0; j < f.order; j++) {
-          MKS_TRY(mks_dslash_fn_field_dev(x_of(t + j), x_of(t + j), MKS_ODD, g));
+          if (!low) MKS_TRY(mks_dslash_fn_field_dev(x_of(t + j), x_of(t + j), MKS_ODD, g));
           allres.push_back(f.res[j + 1]);
         }
         orders[g] += f.order;
         t += f.order;
       }
+      if (low) {
+        std::vector<float2 *> ev, od;
+        for (int j = tg; j < t; j++) {
+          float2 *x = xs32 + (size_t)j * 6 * c.Vh;
+          MKS_TRY(vec_aos_to_soa32(x_of(j), x, 0));
+          ev.push_back(x);
+          od.push_back(x + 3 * c.Vh);
+        }
+        MKS_TRY(dslash32_multi(g, 1, t - tg, ev.data(), od.data()));
+      }
+      t_doe += wall() - td;
     }
     const double t0 = wall();
-    std::vector<double2 *> xp(t);
-    for (int j = 0; j < t; j++) {
-      xp[j] = xs_soa + (size_t)j * 6 * c.Vh;
-      MKS_TRY(vec_aos_to_soa64(x_of(j), xp[j], 0));
-      MKS_TRY(vec_aos_to_soa64(x_of(j), xp[j] + 3 * c.Vh, 1));
+    if (low) {
+      std::vector<float2 *> xp(t);
+      for (int j = 0; j < t; j++) xp[j] = xs32 + (size_t)j * 6 * c.Vh;
+      MKS_TRY(force_dev32(eps, allres.data(), xp.data(), t, orders.data(), n_naiks, c.mom));
+    } else {
+      std::vector<double2 *> xp(t);
+      for (int j = 0; j < t; j++) {
+        xp[j] = xs_soa + (size_t)j * 6 * c.Vh;
+        MKS_TRY(vec_aos_to_soa64(x_of(j), xp[j], 0));
+        MKS_TRY(vec_aos_to_soa64(x_of(j), xp[j] + 3 * c.Vh, 1));
+      }
+      MKS_TRY(force_dev(eps, allres.data(), xp.data(), t, orders.data(), n_naiks, c.mom, nullptr));
     }
-    MKS_TRY(force_dev(eps, allres.data(), xp.data(), t, orders.data(), n_naiks, c.mom, nullptr));
-    r->t_fermion_force += wall() - t0;
+    r->t_fermion_force += wall() - t0 + t_doe;
     r->n_fermion_force++;
     return MKS_OK;
   }
@@ -434,11 +459,14 @@ int mks_rhmc_trajectory(const mks_rhmc_params *p, mks_rhmc_result *r) {
   if (rc >= 0) rc = dev_alloc((void **)&T.tmp, vb);
   if (rc >= 0) rc = dev_alloc((void **)&T.gtmp, (size_t)p->n_pseudo * vb);
   if (rc >= 0) rc = dev_alloc((void **)&T.xs_soa, (size_t)total * 6 * c.Vh * sizeof(double2));
+  if (rc >= 0 && p->prec_force == MKS_PREC_SINGLE)
+    rc = dev_alloc((void **)&T.xs32, (size_t)total * 6 * c.Vh * sizeof(float2));
   if (rc >= 0) rc = T.run();
   dev_free(T.xs);
   dev_free(T.tmp);
   dev_free(T.gtmp);
   dev_free(T.xs_soa);
+  dev_free(T.xs32);
   return rc;
 }
 

@@ -744,6 +744,23 @@ static int alloc_cg_fields(CgFields &f, int nsrc, int prec) {
   return MKS_OK;
 }
 
+int dslash32_multi(int slot, int out_par, int nsrc, float2 *const *in, float2 *const *out) {
+  MKS_TRY(slot_ok(slot));
+  const LinkSlot &sl = ctx().slots[slot];
+  if (!sl.valid || !sl.fat32a) return MKS_ERR_STATE;
+  LinkSet32 L = links32(sl);
+  for (int b0 = 0; b0 < nsrc; b0 += MAXSRC) {
+    const int nb = nsrc - b0 < MAXSRC ? nsrc - b0 : MAXSRC;
+    DslashArgs<VecF32, VecF32, VecF32> a;
+    memset(&a, 0, sizeof a);
+    a.out_par = out_par; a.nsrc = nb;
+    for (int q = 0; q < nb; q++) { a.in[q].p = in[b0 + q]; a.out[q].p = out[b0 + q]; }
+    MKS_TRY((launch_dslash<float, LinkF32, VecF32, VecF32, EPI_PLAIN, 0>(MKS_K_DSLASH_F32, L.fat, L.lng, a,
+                                                                       FinNone())));
+  }
+  return MKS_OK;
+}
+
 // ttt <- D_par D_opar x  (FP64) for the sources listed
 static int apply_DD64(const LinkSlot &sl, int par, int nsrc, double2 *const *x, double2 *const *t,
                       double2 *const *ttt) {
