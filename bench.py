@@ -366,6 +366,14 @@ def gpu_arm(args):
             kernel_ms[name] = {"ms_per_step": t.value / args.steps, "launches_per_step": n.value / args.steps}
     tot_ms, nl = ctypes.c_double(), ctypes.c_longlong()
     lib.mks_timing_get(fam, ctypes.byref(tot_ms), ctypes.byref(nl))
+    # launch shapes the autotuner chose for the sloppy D_eo of this solve
+    shapes = {}
+    G, nb, blk, tma = (ctypes.c_int() for _ in range(4))
+    if lib.mks_tuned_shape(prec, N, ctypes.byref(G), ctypes.byref(nb), ctypes.byref(blk)) == 0:
+        shapes["D"] = {"G": G.value, "NB": nb.value, "block": blk.value}
+    if lib.mks_tuned_shape_epi(prec, N, ctypes.byref(G), ctypes.byref(nb), ctypes.byref(blk),
+                               ctypes.byref(tma)) == 0:
+        shapes["D+epilogue"] = {"G": G.value, "NB": nb.value, "block": blk.value, "tma": tma.value}
     # each source's solution against the plain FP64 GPU CG's solution of the
     # same system (outside the timed region)
     sol_err = []
@@ -439,6 +447,7 @@ def gpu_arm(args):
         "gpu_launches": int(launches),
         "launches_before_timed": int(launches_before),
         "kernel_ms": kernel_ms,
+        "dslash_shapes": shapes,
         "clocks": clk.summary(),
         "link_build_s": t_links,
     }

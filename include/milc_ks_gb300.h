@@ -320,6 +320,11 @@ int mks_bench_dslash(int prec, int nsrc, int parity, int slot, int iters, int fl
  * MKS_ERR_STATE when the pair has not been launched yet. */
 int mks_tuned_shape(int prec, int nsrc, int *G, int *nb, int *block);
 
+/* The same for the launches with the fused CG epilogue (D_eo, axpy and
+ * three dot products in one kernel), tuned separately; *tma = 1 when the
+ * TMA-staged kernel won (then *block = threads per CTA). */
+int mks_tuned_shape_epi(int prec, int nsrc, int *G, int *nb, int *block, int *tma);
+
 /* ------------------------------------------------------------------ */
 /* Gauge side of the RHMC molecular dynamics (mks_gauge.cu).  The library
  * keeps one resident thin-link field (the one the fermion links are built

@@ -2389,3 +2389,14 @@ extern "C" int mks_tuned_shape(int prec, int nsrc, int *G, int *nb, int *block) 
   if (block) *block = s.block;
   return MKS_OK;
 }
+
+extern "C" int mks_tuned_shape_epi(int prec, int nsrc, int *G, int *nb, int *block, int *tma) {
+  if (prec < 0 || prec > 2 || nsrc < 1 || nsrc > MAXSRC) return MKS_ERR_ARG;
+  const Shape &s = g_shape_epi[prec][nsrc];
+  if (s.G == 0) return MKS_ERR_STATE;
+  if (G) *G = s.G;
+  if (nb) *nb = s.NB;
+  if (block) *block = s.block;
+  if (tma) *tma = s.tma;
+  return MKS_OK;
+}
