@@ -206,6 +206,13 @@ struct VecF16 {
   }
 };
 
+// Link loads of D_eo: every link is read once per application, so they are
+// loaded as streaming data (evict-first in L1 and L2) and leave the L2 to the
+// colour vectors, which 16 sites read each (the t-neighbours up to six
+// time slices apart)
+#ifndef MKS_LINK_LD
+#define MKS_LINK_LD __ldcs
+#endif
 struct LinkF64 {
   static constexpr bool scaled = false;
   const double2 *p;  // [par][dir][9][Vh]
@@ -213,7 +220,7 @@ struct LinkF64 {
     const double2 *b = p + ((size_t)(par * 4 + dir) * 9) * Vh + h;
     M3<double> m;
 #pragma unroll
-    for (int k = 0; k < 9; k++) { double2 a = __ldg(b + (size_t)k * Vh); m.e[k / 3][k % 3] = {a.x, a.y}; }
+    for (int k = 0; k < 9; k++) { double2 a = MKS_LINK_LD(b + (size_t)k * Vh); m.e[k / 3][k % 3] = {a.x, a.y}; }
     return m;
   }
 };
@@ -223,11 +230,11 @@ struct LinkF32 {
   const float2 *b;  // [par][dir][Vh]
   __device__ __forceinline__ M3<float> load(int par, int dir, int h, int Vh) const {
     const float4 *pa = a + ((size_t)(par * 4 + dir) * 4) * Vh + h;
-    float2 l = __ldg(b + (size_t)(par * 4 + dir) * Vh + h);
+    float2 l = MKS_LINK_LD(b + (size_t)(par * 4 + dir) * Vh + h);
     M3<float> m;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      float4 q = __ldg(pa + (size_t)k * Vh);
+      float4 q = MKS_LINK_LD(pa + (size_t)k * Vh);
       m.e[(2 * k) / 3][(2 * k) % 3] = {q.x, q.y};
       m.e[(2 * k + 1) / 3][(2 * k + 1) % 3] = {q.z, q.w};
     }
@@ -246,7 +253,7 @@ struct LinkF16 {
     M3<float> m;
 #pragma unroll
     for (int k = 0; k < 2; k++) {
-      uint4 q = __ldg(pa + (size_t)k * Vh);
+      uint4 q = MKS_LINK_LD(pa + (size_t)k * Vh);
       unsigned w[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
       for (int j = 0; j < 4; j++) {
@@ -256,7 +263,7 @@ struct LinkF16 {
         m.e[e / 3][e % 3] = {f.x, f.y};
       }
     }
-    float2 f = __half22float2(__ldg(b + (size_t)(par * 4 + dir) * Vh + h));
+    float2 f = __half22float2(MKS_LINK_LD(b + (size_t)(par * 4 + dir) * Vh + h));
     m.e[2][2] = {f.x, f.y};
     return m;
   }
@@ -265,7 +272,7 @@ struct LinkF16 {
     M3<float> m;
 #pragma unroll
     for (int k = 0; k < 2; k++) {
-      uint4 q = __ldg(pa + (size_t)k * Vh);
+      uint4 q = MKS_LINK_LD(pa + (size_t)k * Vh);
       unsigned w[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
       for (int j = 0; j < 4; j++) {
@@ -275,7 +282,7 @@ struct LinkF16 {
         m.e[e / 3][e % 3] = {f.x * scale, f.y * scale};
       }
     }
-    float2 f = __half22float2(__ldg(b + (size_t)(par * 4 + dir) * Vh + h));
+    float2 f = __half22float2(MKS_LINK_LD(b + (size_t)(par * 4 + dir) * Vh + h));
     m.e[2][2] = {f.x * scale, f.y * scale};
     return m;
   }
