@@ -236,7 +236,9 @@ __device__ __forceinline__ void dslash_body(const LinkT &fat, const LinkT &lng,
           sums[s][2] = d2;
         }
       }
-      a.out[S].store(h, Vh, acc[s]);
+      // the fused-epilogue result is read once, by the next kernel
+      if (EPI == EPI_AXPY) a.out[S].store_stream(h, Vh, acc[s]);
+      else a.out[S].store(h, Vh, acc[s]);
     }
   }
   if (NSUM > 0) {

@@ -147,6 +147,10 @@ struct VecF64 {
 #pragma unroll
     for (int c = 0; c < 3; c++) p[(size_t)c * Vh + h] = make_double2(v.c[c].re, v.c[c].im);
   }
+  __device__ __forceinline__ void store_stream(int h, int Vh, const V3<double> &v) const {
+#pragma unroll
+    for (int c = 0; c < 3; c++) __stcs(p + (size_t)c * Vh + h, make_double2(v.c[c].re, v.c[c].im));
+  }
 };
 struct VecF32 {
   float2 *p;  // [3][Vh]
@@ -164,6 +168,12 @@ struct VecF32 {
   __device__ __forceinline__ void store(int h, int Vh, const V3<float> &v) const {
 #pragma unroll
     for (int c = 0; c < 3; c++) p[(size_t)c * Vh + h] = make_float2(v.c[c].re, v.c[c].im);
+  }
+  // the same as a streaming (evict-first) store, for results that the next
+  // kernel reads once
+  __device__ __forceinline__ void store_stream(int h, int Vh, const V3<float> &v) const {
+#pragma unroll
+    for (int c = 0; c < 3; c++) __stcs(p + (size_t)c * Vh + h, make_float2(v.c[c].re, v.c[c].im));
   }
   __device__ __forceinline__ V3<float> load_mul(int h, int Vh, float f) const {
     V3<float> v = load(h, Vh);
@@ -204,6 +214,7 @@ struct VecF16 {
 #pragma unroll
     for (int c = 0; c < 3; c++) p[(size_t)c * Vh + h] = __floats2half2_rn(v.c[c].re * inv, v.c[c].im * inv);
   }
+  __device__ __forceinline__ void store_stream(int h, int Vh, const V3<float> &v) const { store(h, Vh, v); }
 };
 
 // Link loads of D_eo: every link is read once per application, so they are
