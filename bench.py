@@ -136,8 +136,7 @@ def cpu_baseline(sample_iters=20, threads=None):
 # D_eo family (mean of the plain D and the fused CG-epilogue launch), from
 # ncu captures of this benchmark on GB300 (summaries under profiles/)
 MEASURED_TRAFFIC = {
-    ("single", 8, (32, 32, 32, 64)): 0.5 * (1.802e9 + 2.418e9),
-    ("single", 4, (32, 32, 32, 64)): 0.5 * (1.520e9 + 1.722e9),
+    ("single", 8, (32, 32, 32, 64)): 0.5 * (1.614e9 + 2.095e9),
 }
 
 # FP64 CG iterations to |r|/|b| = 1e-10 on this workload (32^3x64, m = 0.01,
