@@ -36,6 +36,7 @@ struct DslashArgs {
   double coef[MAXSRC];
   const int *skip;            // kernel returns at once when *skip != 0
   const int *src_done;        // per-source: skip the epilogue update when non-zero
+  int rev;                    // plain D only: blocks take the sites in reverse order
   RedScratch red;             // grid reduction scratch (NSUM > 0)
   double *totals;             // [nsrc][NSUM] written by the last block
 };
@@ -122,7 +123,11 @@ __device__ __forceinline__ void dslash_body(const LinkT &fat, const LinkT &lng,
   if (a.skip && *a.skip) return;
   const Geom &g = a.g;
   const int G = a.groups;
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  // a plain D may sweep the sites from the end: it then reads first the part
+  // of its input that the previous kernel wrote last (still in L2) and
+  // leaves the start of its output in L2 for a following forward sweep
+  const int bid = (!TMA && EPI == EPI_PLAIN && a.rev) ? (int)(gridDim.x - 1 - blockIdx.x) : (int)blockIdx.x;
+  const int tid = bid * blockDim.x + threadIdx.x;
   const int h = tid / G, grp = tid - h * G;
   const int Vh = g.Vh;
   const int par = a.out_par, opar = 1 - par;

@@ -424,6 +424,7 @@ static int launch_shape(int family, const LinkT &fat, const LinkT &lng,
                         DslashArgs<InT, OutT, typename EpiLoad<R>::type> &a, const Fin &fin, const Shape &sh) {
   a.groups = sh.G;
   a.g = ctx().geom;
+  if (EPI == EPI_PLAIN) a.rev = 1;
   if constexpr (std::is_same<LinkT, LinkF32>::value && std::is_same<InT, VecF32>::value &&
                 std::is_same<OutT, VecF32>::value) {
     if (sh.tma) {
