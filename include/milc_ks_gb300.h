@@ -146,6 +146,10 @@ int mks_ks_congrad_parity_dev(const double *src_dev, double *dst_dev, double mas
  * once per operator application for all sources.  Replaces
  * ks_congrad_block_parity_gpu (include/imp_ferm_links.h:99-101,
  * generic_ks/d_congrad5_fn_gpu.c:167-305).  res has nsrc entries.
+ * Host arrays that are page-locked and mapped (cudaHostAlloc,
+ * cudaHostRegister) are read and written in place by the solver's kernels;
+ * pageable arrays are staged through device copies.  Either way only the
+ * solved parity's half of each array moves.
  * Returns the largest iteration count or a negative status. */
 int mks_ks_congrad_block_parity(int nsrc, const double *const *src, double *const *dst,
                                 double mass, int slot, const mks_invert_arg *arg,

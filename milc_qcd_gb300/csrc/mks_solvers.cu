@@ -1245,9 +1245,23 @@ static int congrad_block_dev(int nsrc, const double *const *src_dev, double *con
   return MKS_OK;
 }
 
-// host arrays: copy in, solve in batches of MAXSRC, copy out.  A parity
-// solve reads and writes only the sites of its parity, which are one
-// contiguous half of MILC's even-first field: only that half moves.
+// The device address of a page-locked host array mapped into the device
+// address space (cudaHostAlloc / cudaHostRegister), else nullptr (pageable
+// memory, which kernels must not touch).
+static double *mapped_host(const double *p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? (double *)at.devicePointer : nullptr;
+}
+
+// host arrays: solve in batches of MAXSRC.  A parity solve reads and writes
+// only the sites of its parity, which are one contiguous half of MILC's
+// even-first field: only that half moves.  Page-locked arrays are read and
+// written in place by the solver's layout kernels (over the host link, no
+// staging copy); pageable ones are copied in and out.
 static int congrad_block_host(int nsrc, const double *const *src, double *const *dst, double mass, int slot,
                               const mks_invert_arg *arg, mks_invert_result *res) {
   Context &c = ctx();
@@ -1257,7 +1271,15 @@ static int congrad_block_host(int nsrc, const double *const *src, double *const 
   for (int b0 = 0; b0 < nsrc; b0 += MAXSRC) {
     int nb = nsrc - b0 < MAXSRC ? nsrc - b0 : MAXSRC;
     double *ds[MAXSRC], *dd[MAXSRC];
+    bool staged[MAXSRC];
     for (int s = 0; s < nb; s++) {
+      double *ms = mapped_host(src[b0 + s]), *md = mapped_host(dst[b0 + s]);
+      staged[s] = !(ms && md);
+      if (!staged[s]) {
+        ds[s] = ms;
+        dd[s] = md;
+        continue;
+      }
       MKS_TRY(wsv("hsrc" + std::to_string(s), 6 * c.V, &ds[s]));
       MKS_TRY(wsv("hdst" + std::to_string(s), 6 * c.V, &dd[s]));
       MKS_CUDA(cudaMemcpyAsync(ds[s] + off, src[b0 + s] + off, bytes, cudaMemcpyHostToDevice, c.stream));
@@ -1265,7 +1287,8 @@ static int congrad_block_host(int nsrc, const double *const *src, double *const 
     }
     MKS_TRY(congrad_block_dev(nb, ds, dd, mass, slot, arg, res + b0));
     for (int s = 0; s < nb; s++)
-      MKS_CUDA(cudaMemcpyAsync(dst[b0 + s] + off, dd[s] + off, bytes, cudaMemcpyDeviceToHost, c.stream));
+      if (staged[s])
+        MKS_CUDA(cudaMemcpyAsync(dst[b0 + s] + off, dd[s] + off, bytes, cudaMemcpyDeviceToHost, c.stream));
     MKS_CUDA(cudaStreamSynchronize(c.stream));
   }
   return MKS_OK;

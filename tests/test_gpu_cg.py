@@ -166,3 +166,32 @@ def test_block_cg_tma_staged_links(gpu, oracle_cls, monkeypatch, nsrc):
         assert per[k].converged == 1
         _, xo, _ = orc.congrad(fat, lng, srcs[k], np.zeros_like(srcs[k]), 0.03, m.EVEN, 1e-13, 0.0, 2000, 5)
         assert rel(xs[k], xo) < 1e-7, (k, rel(xs[k], xo))
+
+
+@pytest.mark.parametrize("parity", ["EVEN", "ODD"])
+def test_block_cg_page_locked_host_arrays(gpu, oracle_cls, parity):
+    """Page-locked host arrays are read and written in place by the layout
+    kernels (no staging copy): the solutions equal those of pageable arrays
+    bit for bit, and the other parity's half of each destination is kept."""
+    torch = pytest.importorskip("torch")
+    m = gpu
+    orc, fat, lng = _setup(m, oracle_cls)
+    par = getattr(m, parity)
+    nsrc = 3
+    srcs = [m.gen_vector(DIMS, 300 + k, par) for k in range(nsrc)]
+    qic = m.QuarkInvertControl(resid=1e-10, max=2000, nrestart=5, parity=par, prec=m.PREC_SINGLE)
+    V2 = srcs[0].shape[0] // 2
+    solve = slice(0, V2) if par == m.EVEN else slice(V2, None)
+    keep = slice(V2, None) if par == m.EVEN else slice(0, V2)
+    xs = [np.full_like(s, 0.5) for s in srcs]
+    for x in xs:
+        x[solve] = 0.0
+    ref = [x.copy() for x in xs]
+    m.ks_congrad_block_parity(srcs, ref, qic, 0.03)
+    ps = [torch.from_numpy(s).pin_memory().numpy() for s in srcs]
+    px = [torch.from_numpy(x).pin_memory().numpy() for x in xs]
+    it, per = m.ks_congrad_block_parity(ps, px, qic, 0.03)
+    for k in range(nsrc):
+        assert per[k].converged == 1
+        assert np.array_equal(px[k], ref[k])
+        assert np.all(px[k][keep] == 0.5)
