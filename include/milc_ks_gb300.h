@@ -175,7 +175,9 @@ int mks_mat_invert_block_uml(int nsrc, const double *const *src, double *const *
  * 38-250; CPU semantics generic_ks/ks_multicg_offset.c:63-505).  Stops
  * when the smallest shift meets arg->resid, like the CPU code (:381).
  * psim is overwritten on arg->parity (zero initial guess); its other sites
- * are not touched.  res has num_offsets entries.
+ * are not touched.  res has num_offsets entries.  Page-locked, mapped
+ * arrays are read and written in place by the solver's kernels; pageable
+ * ones are staged through device copies.
  * arg->prec selects FP64, or FP32/FP16 shifted updates with FP64 reliable
  * updates of the lowest shift (every shift's solution accumulated in FP64),
  * an FP64 true-residual check of every shift, and a mixed-precision

@@ -2391,6 +2391,15 @@ int mks_ks_multicg_offset_field(const double *src, double *const *psim, const do
   const size_t off = (size_t)par * c.Vh * 6, bytes = c.Vh * 6 * sizeof(double);
   double *ds;
   double *dp[MAXSH];
+  // page-locked, mapped arrays are read and written in place by the layout
+  // kernels; otherwise the source and solutions are staged by copies
+  bool mapped = (ds = mapped_host(src)) != nullptr;
+  for (int j = 0; j < num_offsets && mapped; j++) mapped = (dp[j] = mapped_host(psim[j])) != nullptr;
+  if (mapped) {
+    int it = multishift_dev(ds, dp, offsets, num_offsets, slot, arg, res);
+    MKS_CUDA(cudaStreamSynchronize(c.stream));
+    return it;
+  }
   MKS_TRY(wsv("hsrc0", 6 * c.V, &ds));
   MKS_CUDA(cudaMemcpyAsync(ds + off, src + off, bytes, cudaMemcpyHostToDevice, c.stream));
   for (int j = 0; j < num_offsets; j++) MKS_TRY(wsv("hpsim" + std::to_string(j), 6 * c.V, &dp[j]));
