@@ -107,29 +107,78 @@ def max_over_ranks(value, world, device="cpu"):
 _CPU_CACHE = {}
 
 
-def cpu_baseline(sample_iters=20, threads=None):
-    """MILC's CG (the C oracle restatement of d_congrad5_fn_milc.c) on the host
-    cores: time a bounded window of CG iterations on the full 32^3x64 HISQ
-    problem and extrapolate per solve with the GPU-measured FP64 iteration
-    count.  Links for the CPU run are built by the oracle too."""
-    from oracle.oracle import Oracle
-    import milc_qcd_gb300 as m
-    threads = threads or os.cpu_count()
-    os.environ["OMP_NUM_THREADS"] = str(threads)
+def _cpu_problem():
+    """The 32^3x64 HISQ problem on the host, built by the oracle library alone
+    (the seeded generators of mks_synth.h are compiled into it), so that the
+    reference arm never loads the product library."""
+    from oracle import oracle as O
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
     if _CPU_CACHE.get("dims") != DIMS:
-        U = m.apply_phases(DIMS, m.gen_thin_links(DIMS, SEED_LINKS, LINK_A))
-        orc = Oracle(DIMS)
+        orc = O.Oracle(DIMS)
+        U = orc.rephase(O.gen_thin_links(DIMS, SEED_LINKS, LINK_A))
         t0 = time.time()
         L = orc.hisq_links(U)
         _CPU_CACHE.update(dims=DIMS, orc=orc, fat=L["fat"][0], lng=L["lng"][0], t_links=time.time() - t0,
-                          b=m.gen_vector(DIMS, SEED_SRC, m.EVEN))
-    orc, fat, lng, b = _CPU_CACHE["orc"], _CPU_CACHE["fat"], _CPU_CACHE["lng"], _CPU_CACHE["b"]
-    t_links = _CPU_CACHE["t_links"]
+                          b=O.gen_vector(DIMS, SEED_SRC, O.EVEN))
+    return _CPU_CACHE
+
+
+def cpu_baseline(sample_iters=20, threads=None):
+    """MILC's CG (the C oracle restatement of d_congrad5_fn_milc.c) on the host
+    cores: time a bounded window of CG iterations on the full 32^3x64 HISQ
+    problem (links built by the oracle too)."""
+    threads = threads or os.cpu_count()
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    P = _cpu_problem()
+    orc, fat, lng, b = P["orc"], P["fat"], P["lng"], P["b"]
     t0 = time.time()
-    it, _, _ = orc.congrad(fat, lng, b, np.zeros_like(b), MASS, m.EVEN, 1e-30, 0.0, sample_iters, 1)
+    it, _, _ = orc.congrad(fat, lng, b, np.zeros_like(b), MASS, EVEN, 1e-30, 0.0, sample_iters, 1)
     dt = time.time() - t0
     return {"s_per_iter": dt / max(it, 1), "iters": it, "seconds": dt, "threads": threads,
-            "link_build_s": t_links}
+            "link_build_s": P["t_links"]}
+
+
+def cpu_full_solve(threads=None):
+    """One complete FP64 solve of the first benchmark source to 1e-10 by the
+    oracle's MILC CG on the host cores: its time (no extrapolation) and its
+    solution, against which the GPU solution is checked."""
+    threads = threads or os.cpu_count()
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    P = _cpu_problem()
+    t0 = time.time()
+    it, x, out = P["orc"].congrad(P["fat"], P["lng"], P["b"], np.zeros_like(P["b"]), MASS, EVEN, RESID, 0.0,
+                                  1000, 10)
+    return {"seconds": time.time() - t0, "iters": it, "x": x, "final_rsq": out[0], "threads": threads}
+
+
+def cpu_extras(threads=None):
+    """Labelled host-core timings of the other two workloads, oracle port of
+    MILC's FP64 code: the 11-offset multi-shift CG on 32^3x64 (a bounded
+    window of iterations, extrapolated to the FP64 GPU arm's iteration count)
+    and the HISQ fermion force on 16^3x32 with 6 terms (one full call)."""
+    from oracle import oracle as O
+    threads = threads or os.cpu_count()
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    P = _cpu_problem()
+    sig = 4 * MASS ** 2 + np.logspace(-4, 0, 11)
+    window = 12
+    t0 = time.time()
+    it, _, _ = P["orc"].multicg_offset(P["fat"], P["lng"], P["b"], sig, EVEN, 1e-30, window, 1)
+    dt = time.time() - t0
+    ms = {"s_per_iter": dt / max(it, 1), "window_iters": it, "window_s": dt,
+          "extrapolated_s_per_solve": dt / max(it, 1) * FP64_MULTISHIFT_ITERS_32C64,
+          "sample": "%d iterations of MILC's 11-offset multi-shift CG (oracle port, FP64) on 32^3x64, "
+                    "extrapolated to the FP64 GPU arm's %d iterations" % (it, FP64_MULTISHIFT_ITERS_32C64)}
+    fdims = (16, 16, 16, 32)
+    forc = O.Oracle(fdims)
+    U = forc.rephase(O.gen_thin_links(fdims, 77, LINK_A))
+    xxx = np.stack([O.gen_vector(fdims, 300 + j, O.EVENANDODD) for j in range(6)])
+    t0 = time.time()
+    forc.fermion_force_hisq(U, 0.01, np.linspace(0.1, 1.0, 6), xxx)
+    force = {"s_per_call": time.time() - t0,
+             "sample": "one HISQ fermion force call (oracle port of MILC's FP64 force, links smeared inside), "
+                       "16^3x32, 6 terms"}
+    return {"multishift_11_offsets_32c64": ms, "hisq_force_16c32_6terms": force, "threads": threads}
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the multi-source
@@ -143,33 +192,44 @@ MEASURED_TRAFFIC = {
 # seeded links and source): MILC's CG and the GPU FP64 arm take the same
 # count (identical recurrences), measured by the GPU arm on GB300.
 FP64_ITERS_32C64 = 279
+# the same for the FP64 11-offset multi-shift solve of the first source
+FP64_MULTISHIFT_ITERS_32C64 = 277
+EVEN, ODD, EVENANDODD = 0x02, 0x01, 0x03
 
 
 def reference_arm(args):
+    """MILC's FP64 CG (oracle port of d_congrad5_fn_milc.c) on the host cores.
+    Loads only the oracle library: inputs come from the oracle's copy of the
+    seeded generators.  A step is one bounded window of CG iterations on the
+    full lattice; ms_per_step is the measured window time, and `value` the
+    per-solve time extrapolated from the measured rate to the FP64 iteration
+    count (labelled in cpu_baseline.sample)."""
     rank, world = dist_env()
     if rank != 0:
         return
     iters = args.ref_iters
-    # W untimed and K timed samples of a bounded window of MILC's CG
-    # iterations on the full lattice (one sample ~ 1-2 s on 16 cores)
     for _ in range(max(args.warmup, 1)):
         cpu_baseline(sample_iters=2)
     samples = [cpu_baseline(sample_iters=args.cpu_iters) for _ in range(max(args.steps, 1))]
-    base = samples[-1]
-    base["s_per_iter"] = sum(b["s_per_iter"] for b in samples) / len(samples)
-    base["iters"] = sum(b["iters"] for b in samples)
-    base["seconds"] = sum(b["seconds"] for b in samples)
-    per_solve = base["s_per_iter"] * iters
+    threads = samples[-1]["threads"]
+    s_per_iter = sum(b["seconds"] for b in samples) / sum(b["iters"] for b in samples)
+    window_ms = 1e3 * sum(b["seconds"] for b in samples) / len(samples)
+    per_solve = s_per_iter * iters
+    sample = ("%d windows of %d iterations of MILC's FEWSUMS CG on the full lattice (%.1f s measured, %.0f ms per "
+              "window); value = measured s/iteration x %d iterations (extrapolated)"
+              % (len(samples), args.cpu_iters, sum(b["seconds"] for b in samples), window_ms, iters))
     line = {"impl": "reference", "metric": METRIC, "value": per_solve, "unit": "s/solve", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_solve * 1e3,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": window_ms,
+            "step": "one window of %d CG iterations (measured)" % args.cpu_iters,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded exp(i 0.3 H) thin links, HISQ smearing, Gaussian sources)",
             "config": {"workload": "HISQ CG 32^3x64 m=0.01 |r|/|b|=1e-10, single source, FP64",
                        "lattice": list(DIMS), "mass": MASS, "resid": RESID},
-            "cpu_baseline": {"value": per_solve, "unit": "s/solve", "cores": base["threads"], "kind": "port",
-                             "sample": "%d CG iterations of MILC's FEWSUMS CG on the full lattice (%.1f s), "
-                                       "extrapolated to %d iterations" % (base["iters"], base["seconds"], iters)},
+            "cpu_baseline": {"value": per_solve, "unit": "s/solve", "cores": threads, "kind": "port",
+                             "sample": sample},
             "e2e": {"value": per_solve, "unit": "s/solve", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if not args.no_extras:
+        line["extras"] = cpu_extras(threads)
     print(json.dumps(line), flush=True)
 
 
@@ -373,15 +433,6 @@ def gpu_arm(args):
     if lib.mks_tuned_shape_epi(prec, N, ctypes.byref(G), ctypes.byref(nb), ctypes.byref(blk),
                                ctypes.byref(tma)) == 0:
         shapes["D+epilogue"] = {"G": G.value, "NB": nb.value, "block": blk.value, "tma": tma.value}
-    # each source's solution against the plain FP64 GPU CG's solution of the
-    # same system (outside the timed region)
-    sol_err = []
-    for k in range(N):
-        d64k = torch.zeros_like(d_src[k])
-        m.check(lib.mks_ks_congrad_parity_dev(d_src[k].data_ptr(), d64k.data_ptr(), MASS, 0,
-                                              ctypes.byref(arg64), ctypes.byref(_lib.InvertResult())), "fp64 ref")
-        xr = d64k.cpu().numpy()[:V // 2]
-        sol_err.append(float(np.linalg.norm(x_host[k][:V // 2] - xr) / np.linalg.norm(xr)))
     dslash_ms = tot_ms.value / max(nl.value, 1)
     Vh = V // 2
     if prec == m.PREC_HALF:
@@ -405,7 +456,7 @@ def gpu_arm(args):
     # library's layout kernels read the sources and guesses and write the solutions
     # over the host link inside the timed region (the parity halves counted below).
     # Each step gets its own zero initial guess, prepared before the clock starts.
-    e2e_steps = max(1, min(args.steps, 3))
+    e2e_steps = max(1, args.steps)
     h_src = [torch.from_numpy(s).pin_memory() for s in srcs]
     h_dst = [[torch.zeros_like(t).pin_memory() for t in h_src] for _ in range(e2e_steps)]
     DPv = _lib.DP * N
@@ -434,7 +485,6 @@ def gpu_arm(args):
         "speedup_vs_fp64_plain": t_fp64 / per_src,
         "iters": iters, "reliable_updates": reliable, "final_rsq_max": final_rsq, "converged": converged,
         "cg_gflops": cg_gflops,
-        "solution_rel_error_vs_fp64_cg": sol_err,
         "dslash_gbs": {"f32_single_rhs": gbs32, "f32_ms": ms32.value, "f64_ms": ms64.value,
                        "f64_gflops": 1146.0 * Vh / (ms64.value * 1e-3) / 1e9},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -455,13 +505,37 @@ def gpu_arm(args):
     if not args.no_extras:
         line["extras"] = extras(m, lib, _lib, torch, srcs)
     if not args.no_cpu and world == 1:
-        base = cpu_baseline(sample_iters=args.cpu_iters)
-        cpu_per = base["s_per_iter"] * it64
-        line["cpu_baseline"] = {"value": cpu_per, "unit": "s/solve", "cores": base["threads"], "kind": "port",
-                                "sample": "%d iterations of MILC's FP64 CG (oracle port) on the full lattice in "
-                                          "%.1f s, extrapolated to the GPU FP64 iteration count %d"
-                                          % (base["iters"], base["seconds"], it64)}
+        # the oracle (MILC's FP64 CG restated in C) solves the first source
+        # completely on the host cores: a full-solve CPU time, and the
+        # reference solution for the GPU's; every GPU solution's true residual
+        # is recomputed with the oracle's D (its own links, built on the host)
+        full = cpu_full_solve()
+        line["cpu_baseline"] = {"value": full["seconds"], "unit": "s/solve", "cores": full["threads"],
+                                "kind": "port",
+                                "sample": "one complete FP64 solve of the first source to 1e-10 by the oracle port "
+                                          "of MILC's CG (%d iterations, no extrapolation)" % full["iters"]}
+        line["oracle_check"] = oracle_check(x_host, srcs, full)
     print(json.dumps(line), flush=True)
+
+
+def oracle_check(x_host, srcs, full):
+    """Each GPU solution against the oracle: the FP64 true residual
+    |b - (4m^2 - D_eo D_oe) x| / |b| recomputed with the oracle's D for every
+    source, and the relative solution error against the oracle's full FP64 CG
+    solve of the first source."""
+    P = _cpu_problem()
+    orc, fat, lng = P["orc"], P["fat"], P["lng"]
+    Vh = srcs[0].shape[0] // 2
+    res = []
+    for x, b in zip(x_host, srcs):
+        Dx = orc.dslash(fat, lng, orc.dslash(fat, lng, x, ODD), EVEN)
+        r = b[:Vh] - (4 * MASS ** 2 * x[:Vh] - Dx[:Vh])
+        res.append(float(np.linalg.norm(r) / np.linalg.norm(b[:Vh])))
+    xo = full["x"][:Vh]
+    return {"true_residual_by_oracle_D": res,
+            "solution_rel_error_vs_oracle_cg_src0": float(np.linalg.norm(x_host[0][:Vh] - xo) / np.linalg.norm(xo)),
+            "oracle_cg_iters_src0": full["iters"],
+            "links": "GPU HISQ smearing (solve) vs oracle HISQ smearing (check), same seeded thin links"}
 
 
 # 2+1+1 HISQ RHMC trajectory (the molecular-dynamics workload): 48^3x96,

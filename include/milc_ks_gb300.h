@@ -123,10 +123,12 @@ int mks_dslash_fn_field_dev(const double *src_dev, double *dst_dev, int parity, 
  * allocates nothing: its staging lives in a fixed 32 MiB device array that
  * every GPU loading the library keeps until exit, which limits it to
  * lattices of at most 349,525 sites (MKS_ERR_ARG beyond).  All calls share
- * that array; calls that overlap on the GPU race on it.  The first call on a
- * device looks up the array's device address (cudaGetSymbolAddress); make
- * that first call before any stream capture.  Links must already be loaded
- * in `slot`. */
+ * that array; calls that overlap on the GPU race on it.  mks_init looks up
+ * the array's device address (cudaGetSymbolAddress, with the library's
+ * device current) and loads the kernels this entry point launches, so the
+ * array is resident from mks_init on and no call of this entry point loads
+ * code or takes device memory; call mks_init before handing the device
+ * memory to a pool.  Links must already be loaded in `slot`. */
 int mks_dslash_fn_field_dev_noalloc(const double *src_dev, double *dst_dev, int parity, int slot);
 
 /* ------------------------------------------------------------------ */

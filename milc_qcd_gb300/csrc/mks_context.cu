@@ -146,10 +146,18 @@ int red_check() {
   MKS_CUDA(cudaStreamSynchronize(c.stream));
   if (!e) return MKS_OK;
   MKS_CUDA(cudaMemsetAsync(c.red.err, 0, sizeof(int), c.stream));
-  if (e & 2)
-    snprintf(g_errmsg, sizeof g_errmsg, "D_eo link staging did not complete within its wait limit");
-  else
-    snprintf(g_errmsg, sizeof g_errmsg, "reduction scratch too small for a launch (internal sizing error)");
+  if (e & 6) {
+    // value 2: a TMA-staged D_eo tile gave up waiting for its links (it
+    // computed nothing); value 4: its copies were still in flight after the
+    // second wait.  The staged kernel is off from now on.
+    tma_disable();
+    snprintf(g_errmsg, sizeof g_errmsg,
+             "TMA-staged D_eo: link staging did not complete within its wait limit (%s); the staged kernel is "
+             "switched off for this process",
+             (e & 4) ? "copies still in flight" : "tile skipped");
+    return MKS_ERR_TIMEOUT;
+  }
+  snprintf(g_errmsg, sizeof g_errmsg, "reduction scratch too small for a launch (internal sizing error)");
   return MKS_ERR_CUDA;
 }
 
@@ -361,7 +369,7 @@ const char *mks_error_string(int status) {
   case MKS_ERR_CUDA: return g_errmsg[0] ? g_errmsg : "CUDA error";
   case MKS_ERR_NOMEM: return g_errmsg[0] ? g_errmsg : "device allocation failed";
   case MKS_ERR_STATE: return "library not initialised, lattice not set or links not loaded";
-  case MKS_ERR_TIMEOUT: return "bounded device wait gave up";
+  case MKS_ERR_TIMEOUT: return g_errmsg[0] ? g_errmsg : "bounded device wait gave up";
   case MKS_ERR_NUMERIC: return "non-finite value in a solver recurrence";
   case MKS_ERR_UNSUPPORTED: return "unsupported option";
   default: return "unknown status";
@@ -388,6 +396,12 @@ int mks_init(int device) {
   c.ev_pool.resize(2 * EV_POOL);
   c.ev_family.resize(EV_POOL);
   for (auto &e : c.ev_pool) MKS_CUDA(cudaEventCreate(&e));
+  // the allocation-free D_eo takes no device memory after this point: its
+  // fixed array and the kernels it launches are loaded now
+  cudaFuncAttributes fa;
+  MKS_CUDA(cudaFuncGetAttributes(&fa, k_vec_aos_to_soa));
+  MKS_CUDA(cudaFuncGetAttributes(&fa, k_vec_soa_to_aos));
+  MKS_TRY(noalloc_prepare());
   c.initialised = true;
   return MKS_OK;
 }
@@ -415,6 +429,7 @@ int mks_finalize(void) {
   for (auto &e : c.ev_pool) cudaEventDestroy(e);
   c.ev_pool.clear();
   cudaStreamDestroy(c.stream);
+  noalloc_forget();
   c = Context();
   return MKS_OK;
 }

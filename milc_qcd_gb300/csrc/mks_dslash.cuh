@@ -115,10 +115,14 @@ struct TileSmem {
   }
 };
 
+// live = false (a TMA tile whose staged links did not arrive): the thread
+// computes and writes nothing but still takes part in the grid reduction
+// with zero sums, so the arrival counters return to zero as in every launch
 template <typename R, class LinkT, class InT, class OutT, int NB, int EPI, int NSUM, class Fin, bool TMA = false>
 __device__ __forceinline__ void dslash_body(const LinkT &fat, const LinkT &lng,
                                             const DslashArgs<InT, OutT, typename EpiLoad<R>::type> &a,
-                                            const Fin &fin, const TileSmem ts = TileSmem{nullptr, 0}) {
+                                            const Fin &fin, const TileSmem ts = TileSmem{nullptr, 0},
+                                            const bool live = true) {
   typedef typename EpiLoad<R>::type EpiT;
   if (a.skip && *a.skip) return;
   const Geom &g = a.g;
@@ -140,7 +144,7 @@ __device__ __forceinline__ void dslash_body(const LinkT &fat, const LinkT &lng,
 #ifndef MKS_EPI_PREFETCH
 #define MKS_EPI_PREFETCH 1  // measured: 3 % faster 8-source CG on GB300
 #endif
-  if (MKS_EPI_PREFETCH && EPI == EPI_AXPY && grp == 0 && (h & 15) == 0 && h < Vh) {
+  if (MKS_EPI_PREFETCH && EPI == EPI_AXPY && grp == 0 && (h & 15) == 0 && h < Vh && live) {
     // the epilogue operands are needed only after the 16 neighbour terms:
     // start bringing them into L2 now (one thread per 16 sites)
 #pragma unroll
@@ -152,7 +156,7 @@ __device__ __forceinline__ void dslash_body(const LinkT &fat, const LinkT &lng,
       }
     }
   }
-  if (h < Vh) {
+  if (h < Vh && live) {
     int x, y, z, t;
     site_coords(g, par, h, x, y, z, t);
     V3<R> acc[NB];
@@ -352,9 +356,15 @@ __device__ __forceinline__ bool tile_segment(const Geom &g, int T, int R, int h0
 // FP32 multi-source D_eo with the links of each tile of T sites staged in
 // shared memory by the TMA engine (one thread per site and source, G
 // threads per site; blockDim = T G).  Warp 0 issues the bulk copies, every
-// thread waits on the tile's mbarrier with a bounded poll; a wait that runs
-// out sets bit 2 of the reduction error flag (read by the host at each poll)
-// and the kernel still returns.
+// thread waits on the tile's mbarrier with a bounded poll.  A thread whose
+// wait runs out ORs the value 2 (bit 1) into the reduction error flag, which
+// the host reads at its next poll, waits once more (bounded) for the copies
+// in flight to land in the block's shared memory, and then computes and
+// writes nothing: it only takes part in the grid reduction with zero sums so
+// that the reduction's arrival counters end at zero.  If the second wait
+// runs out too, it ORs in the value 4 (bit 2).  The host treats either bit
+// as fatal for the staged kernel: it stops using it for the rest of the
+// process and the solver call repeats its work with the plain kernel.
 template <int EPI, int NSUM, class Fin>
 __global__ void __launch_bounds__(256)
 k_dslash_tma(const LinkF32 fat, const LinkF32 lng, const DslashArgs<VecF32, VecF32, VecF32> a, const Fin fin,
@@ -385,11 +395,14 @@ k_dslash_tma(const LinkF32 fat, const LinkF32 lng, const DslashArgs<VecF32, VecF
         bulk_g2s(reg + (size_t)64 * T + 8 * loc0, L.b + (size_t)(sp * 4 + mu) * Vh + src0, (uint32_t)cnt * 8u, &bar);
     }
   }
+  bool live = true;
   if (!mbar_wait_bounded(&bar, 0, 1 << 22)) {
+    live = false;
     if (a.red.err) atomicOr(a.red.err, 2);
-    mbar_wait_bounded(&bar, 0, 1 << 22);  // let copies in flight land before the block exits
+    // let copies in flight land before the block's shared memory is released
+    if (!mbar_wait_bounded(&bar, 0, 1 << 22) && a.red.err) atomicOr(a.red.err, 4);
   }
-  dslash_body<float, LinkF32, VecF32, VecF32, 1, EPI, NSUM, Fin, true>(fat, lng, a, fin, TileSmem{tsm, T});
+  dslash_body<float, LinkF32, VecF32, VecF32, 1, EPI, NSUM, Fin, true>(fat, lng, a, fin, TileSmem{tsm, T}, live);
 }
 
 }  // namespace mks

@@ -311,7 +311,12 @@ struct RedScratch {
   size_t max_count;
   int *err;             // set on the device when a launch would overrun the scratch
 };
-int red_check();  // MKS_ERR_CUDA (and clears the flag) if a reduction overran
+// reads and clears the device error flag: MKS_ERR_CUDA if a reduction
+// overran its scratch, MKS_ERR_TIMEOUT (after tma_disable) if a TMA-staged
+// D_eo tile gave up waiting for its links
+int red_check();
+// switch the TMA-staged D_eo off for the rest of the process (mks_solvers.cu)
+void tma_disable();
 
 // gauge side of the molecular dynamics (mks_gauge.cu), on the resident
 // thin links and momenta
@@ -419,6 +424,11 @@ void ws_free_all();
 int ensure_red(int nsum, int blocks);
 
 inline int grid_for(size_t n, int block) { return (int)((n + block - 1) / block); }
+
+// allocation-free D_eo (mks_noalloc.cu): resolve its fixed device array and
+// load its kernel at mks_init; forget the address at mks_finalize
+int noalloc_prepare();
+void noalloc_forget();
 
 // layout conversion (mks_context.cu)
 int vec_aos_to_soa64(const double *aos_dev, double2 *soa, int par);   // one parity from a full AoS field

@@ -367,6 +367,27 @@ static void shapes_reset() {
   memset(g_shape_epi, 0, sizeof g_shape_epi);
 }
 
+// The TMA-staged kernel is switched off for the rest of the process once one
+// of its staging waits ran out (red_check reports it): the shapes that use
+// it are dropped (re-chosen without it at the next launch) with the graphs
+// that bake them in, and the solver entry points repeat their work once.
+static bool g_tma_off = false, g_tma_retry = false;
+void tma_disable() {
+  g_tma_off = true;
+  g_tma_retry = true;
+  for (auto *tab : {g_shape, g_shape_epi})
+    for (int p = 0; p < 3; p++)
+      for (int n = 0; n <= MAXSRC; n++)
+        if (tab[p][n].tma) tab[p][n] = Shape{0, 0, 0, 0};
+  graphs_free_all();
+}
+// true once after tma_disable: the failed call may be repeated
+static bool take_tma_retry() {
+  const bool r = g_tma_retry;
+  g_tma_retry = false;
+  return r;
+}
+
 static Shape default_shape(int nsrc) {
   if (nsrc <= 1) return {1, 1, 256, 0};
   if (nsrc <= 2) return {1, 2, 256, 0};
@@ -547,7 +568,7 @@ static int tune_shape(const LinkT &fat, const LinkT &lng, int nsrc, Shape *best)
     int G = 1;
     while (G < nsrc) G *= 2;
     int T, Rr;
-    if (nsrc >= 2 && tma_tile(c.geom, G, &T, &Rr)) {
+    if (nsrc >= 2 && !g_tma_off && tma_tile(c.geom, G, &T, &Rr)) {
       Shape sh = {G, 1, T * G, 1};
       float tot = 0;
       for (int it = 0; it < 4; it++) {
@@ -591,7 +612,7 @@ static bool shape_override(int prec, int nsrc, Shape *out) {
       return true;
     }
     int T, Rr;
-    if (sscanf(item.c_str(), "%d:%d:%d:%d:", &p, &n, &G, &NB) == 4 && item.size() > 4 &&
+    if (!g_tma_off && sscanf(item.c_str(), "%d:%d:%d:%d:", &p, &n, &G, &NB) == 4 && item.size() > 4 &&
         item.compare(item.size() - 4, 4, ":tma") == 0 && p == MKS_PREC_SINGLE && p == prec && n == nsrc &&
         NB == 1 && G >= nsrc && G <= 16 && (G & (G - 1)) == 0 && tma_tile(ctx().geom, G, &T, &Rr)) {
       *out = {G, 1, T * G, 1};
@@ -1239,7 +1260,14 @@ static int congrad_block_dev(int nsrc, const double *const *src_dev, double *con
     MKS_TRY(vec_aos_to_soa64(src_dev[s], f.src[s], par));
     MKS_TRY(vec_aos_to_soa64(dst_dev[s], f.x[s], par));
   }
-  MKS_TRY(block_cg(slot, par, nsrc, mass, arg, f, res));
+  int rc = block_cg(slot, par, nsrc, mass, arg, f, res);
+  if (rc == MKS_ERR_TIMEOUT && take_tma_retry()) {
+    // the staged D_eo kernel gave up and is now off: solve again from the
+    // caller's initial guess (dst is written only on success)
+    for (int s = 0; s < nsrc; s++) MKS_TRY(vec_aos_to_soa64(dst_dev[s], f.x[s], par));
+    rc = block_cg(slot, par, nsrc, mass, arg, f, res);
+  }
+  MKS_TRY(rc);
   for (int s = 0; s < nsrc; s++) MKS_TRY(vec_soa64_to_aos(f.x[s], dst_dev[s], par));
   MKS_CUDA(cudaStreamSynchronize(ctx().stream));
   return MKS_OK;
@@ -2212,8 +2240,9 @@ static int multishift_multi_core(const LinkSlot &sl, int par, int nf, const doub
 
 // nf fields on one slot: offsets, psim_dev and res are the fields' lists one
 // after the other (num_offsets[f] entries each)
-static int multishift_multi_dev(int nf, const double *const *src_dev, const int *num_offsets, const double *offsets,
-                                double *const *psim_dev, int slot, const mks_invert_arg *arg, mks_invert_result *res) {
+static int multishift_multi_dev_once(int nf, const double *const *src_dev, const int *num_offsets,
+                                     const double *offsets, double *const *psim_dev, int slot,
+                                     const mks_invert_arg *arg, mks_invert_result *res) {
   Context &c = ctx();
   const LinkSlot &sl = c.slots[slot];
   int par;
@@ -2272,8 +2301,8 @@ static int multishift_multi_dev(int nf, const double *const *src_dev, const int 
   return mx;
 }
 
-static int multishift_dev(const double *src_dev, double *const *psim_dev, const double *offsets, int nsh, int slot,
-                          const mks_invert_arg *arg, mks_invert_result *res) {
+static int multishift_dev_once(const double *src_dev, double *const *psim_dev, const double *offsets, int nsh,
+                               int slot, const mks_invert_arg *arg, mks_invert_result *res) {
   Context &c = ctx();
   const LinkSlot &sl = c.slots[slot];
   int par;
@@ -2333,6 +2362,22 @@ static int multishift_dev(const double *src_dev, double *const *psim_dev, const 
   int mx = 0;
   for (int j = 0; j < nsh; j++) mx = res[j].final_iters > mx ? res[j].final_iters : mx;
   return mx;
+}
+
+// The multi-shift entry cores, repeated once when the staged D_eo kernel gave
+// up during the call (it is off afterwards; the solutions are outputs only).
+static int multishift_dev(const double *src_dev, double *const *psim_dev, const double *offsets, int nsh, int slot,
+                          const mks_invert_arg *arg, mks_invert_result *res) {
+  int rc = multishift_dev_once(src_dev, psim_dev, offsets, nsh, slot, arg, res);
+  if (rc == MKS_ERR_TIMEOUT && take_tma_retry()) rc = multishift_dev_once(src_dev, psim_dev, offsets, nsh, slot, arg, res);
+  return rc;
+}
+static int multishift_multi_dev(int nf, const double *const *src_dev, const int *num_offsets, const double *offsets,
+                                double *const *psim_dev, int slot, const mks_invert_arg *arg, mks_invert_result *res) {
+  int rc = multishift_multi_dev_once(nf, src_dev, num_offsets, offsets, psim_dev, slot, arg, res);
+  if (rc == MKS_ERR_TIMEOUT && take_tma_retry())
+    rc = multishift_multi_dev_once(nf, src_dev, num_offsets, offsets, psim_dev, slot, arg, res);
+  return rc;
 }
 
 }  // namespace mks

@@ -182,89 +182,192 @@ static double rel_residue(const orc_lat *L, const double *p, const double *q, in
   return sqrt(2 * residue / L->V);
 }
 
-/* ---------------- CG: generic_ks/d_congrad5_fn_milc.c:61-407 (FEWSUMS) ---------------- */
-int orc_congrad(const orc_lat *L, const double *fat, const double *lng,
-                const double *src, double *dest, double mass, int parity,
-                double resid, double relresid, int niter, int max_restarts, double out[7]) {
+/* D on nsrc fields at once (links read once per site for all of them); per
+   field the arithmetic is orc_dslash's, statement for statement, so each
+   output equals orc_dslash's bit for bit.  In place allowed (src == dst). */
+static void orc_dslash_multi(const orc_lat *L, const double *fat, const double *lng, int nsrc,
+                             double *const *src, double *const *dst, int parity) {
+  size_t lo = 0, hi = L->V;
+  if (parity == ORC_EVEN) hi = L->Vh;
+  else if (parity == ORC_ODD) lo = L->Vh;
+  const size_t n = hi - lo;
+  double *out = (double *)malloc((size_t)nsrc * n * 6 * sizeof(double));
+#pragma omp parallel for schedule(static)
+  for (long long k = 0; k < (long long)n; k++) {
+    size_t i = lo + (size_t)k;
+    const size_t *nb = L->nb + 16 * i;
+    for (int s = 0; s < nsrc; s++) {
+      const double *sv = src[s];
+      double acc[6] = {0}, lacc[6] = {0}, t[6];
+      for (int mu = 0; mu < 4; mu++) {
+        mat_vec(fat + (4 * i + mu) * 18, sv + 6 * nb[mu], t);
+        for (int q = 0; q < 6; q++) acc[q] += t[q];
+        mat_vec(lng + (4 * i + mu) * 18, sv + 6 * nb[8 + mu], t);
+        for (int q = 0; q < 6; q++) lacc[q] += t[q];
+      }
+      for (int mu = 0; mu < 4; mu++) {
+        size_t b1 = nb[7 - mu], b3 = nb[8 + 7 - mu];
+        adj_mat_vec(fat + (4 * b1 + mu) * 18, sv + 6 * b1, t);
+        for (int q = 0; q < 6; q++) acc[q] -= t[q];
+        adj_mat_vec(lng + (4 * b3 + mu) * 18, sv + 6 * b3, t);
+        for (int q = 0; q < 6; q++) lacc[q] -= t[q];
+      }
+      for (int q = 0; q < 6; q++) out[((size_t)s * n + (size_t)k) * 6 + q] = acc[q] + lacc[q];
+    }
+  }
+  for (int s = 0; s < nsrc; s++) memcpy(dst[s] + 6 * lo, out + (size_t)s * n * 6, n * 6 * sizeof(double));
+  free(out);
+}
+
+/* ---------------- CG: generic_ks/d_congrad5_fn_milc.c:61-407 (FEWSUMS) ----------------
+ * nsrc independent solves run in lockstep: each round applies M^dag M once
+ * to every running source (to dest at a restart, to cg_p in an iteration)
+ * with one multi-field D, then runs that source's part of MILC's loop.
+ * Every source follows MILC's recurrences, restarts and stopping rule on
+ * its own, in MILC's order of operations, so its result and iteration count
+ * are those of a solve by itself; orc_congrad is the one-source case.  Sums
+ * over sites are sequential, as in MILC's single-thread loop. */
+typedef struct {
+  const double *src;
+  double *dest, *ttt, *cg_p, *res;
+  double source_norm, size_r, size_relr, final_rsq, final_relrsq;
+  double rsq, relrsq, actual_rsq, oldrsq;
+  int iteration, nrestart, converged, mode, running;  /* mode 0: check, 1: restart, 2: iterate */
+} orc_cg_state;
+
+int orc_congrad_multi(const orc_lat *L, const double *fat, const double *lng, int nsrc,
+                      const double *const *srcs, double *const *dests, double mass, int parity,
+                      double resid, double relresid, int niter, int max_restarts, double *out7) {
   size_t lo, hi;
   par_range(L, parity, &lo, &hi);
   int otherparity = parity == ORC_EVEN ? ORC_ODD : ORC_EVEN;
   double rsqmin = resid * resid, relrsqmin = relresid * relresid;
   int max_cg = max_restarts * niter;
   double msq_x4 = 4.0 * mass * mass;
-  double source_norm = 0;
-  for (size_t i = 6 * lo; i < 6 * hi; i++) source_norm += src[i] * src[i];
-  int iteration = 0, nrestart = 0, converged = 1;
-  double size_r = 0, size_relr = 1.0, final_rsq = 0, final_relrsq = 0;
-  double rsq = 0, relrsq = 1.0, actual_rsq = 999., oldrsq, pkp, c_tr, c_tt;
-  if (source_norm == 0.0) {
-    memset(dest + 6 * lo, 0, (hi - lo) * 6 * sizeof(double));
-    if (out) { for (int k = 0; k < 7; k++) out[k] = 0; out[6] = 1; }
-    return 0;
-  }
   size_t n6 = 6 * L->V;
-  double *ttt = (double *)calloc(n6, sizeof(double));
-  double *cg_p = (double *)calloc(n6, sizeof(double));
-  double *res = (double *)calloc(n6, sizeof(double));
-  while (1) {
-    if ((iteration % niter == 0) ||
-        ((rsqmin <= 0 || rsqmin > size_r) && (relrsqmin <= 0 || relrsqmin > size_relr))) {
-      rsq = 0;
-      orc_dslash(L, fat, lng, dest, ttt, otherparity);
-      orc_dslash(L, fat, lng, ttt, ttt, parity);
+  orc_cg_state *S = (orc_cg_state *)calloc((size_t)nsrc, sizeof(orc_cg_state));
+  double **vin = (double **)malloc((size_t)nsrc * sizeof(double *));
+  double **vout = (double **)malloc((size_t)nsrc * sizeof(double *));
+  int nrun = 0;
+  for (int s = 0; s < nsrc; s++) {
+    orc_cg_state *q = &S[s];
+    q->src = srcs[s];
+    q->dest = dests[s];
+    for (size_t i = 6 * lo; i < 6 * hi; i++) q->source_norm += q->src[i] * q->src[i];
+    q->converged = 1;
+    q->size_relr = 1.0;
+    q->relrsq = 1.0;
+    q->actual_rsq = 999.;
+    if (q->source_norm == 0.0) {
+      memset(q->dest + 6 * lo, 0, (hi - lo) * 6 * sizeof(double));
+      continue;
+    }
+    q->ttt = (double *)calloc(n6, sizeof(double));
+    q->cg_p = (double *)calloc(n6, sizeof(double));
+    q->res = (double *)calloc(n6, sizeof(double));
+    q->running = 1;
+    nrun++;
+  }
+  while (nrun > 0) {
+    int nd = 0;
+    for (int s = 0; s < nsrc; s++) {
+      orc_cg_state *q = &S[s];
+      if (!q->running) continue;
+      if (q->mode == 0)
+        q->mode = ((q->iteration % niter == 0) ||
+                   ((rsqmin <= 0 || rsqmin > q->size_r) && (relrsqmin <= 0 || relrsqmin > q->size_relr))) ? 1 : 2;
+      vin[nd] = q->mode == 1 ? q->dest : q->cg_p;
+      vout[nd] = q->ttt;
+      nd++;
+    }
+    orc_dslash_multi(L, fat, lng, nd, vin, vout, otherparity);
+    orc_dslash_multi(L, fat, lng, nd, vout, vout, parity);
+#pragma omp parallel for schedule(dynamic, 1) reduction(- : nrun)
+    for (int s = 0; s < nsrc; s++) {
+      orc_cg_state *q = &S[s];
+      if (!q->running) continue;
+      double *ttt = q->ttt, *cg_p = q->cg_p, *res = q->res, *dest = q->dest;
+      const double *src = q->src;
+      if (q->mode == 1) {
+        double rsq = 0;
+        for (size_t i = 6 * lo; i < 6 * hi; i++) {
+          ttt[i] = ttt[i] + (-msq_x4) * dest[i];
+          res[i] = src[i] + ttt[i];
+          cg_p[i] = res[i];
+          rsq += res[i] * res[i];
+        }
+        q->rsq = rsq;
+        q->actual_rsq = rsq;
+        if (relrsqmin > 0) q->relrsq = rel_residue(L, res, dest, parity);
+        q->final_rsq = rsq / q->source_norm;
+        q->final_relrsq = q->relrsq;
+        q->iteration++;
+        if (q->iteration >= max_cg || q->nrestart >= max_restarts ||
+            ((rsqmin <= 0 || rsqmin > q->final_rsq) && (relrsqmin <= 0 || relrsqmin > q->final_relrsq))) {
+          q->running = 0;
+          nrun--;
+          continue;
+        }
+        q->nrestart++;
+        q->mode = 2;  /* MILC's loop goes on to the iteration without a new check */
+        continue;
+      }
+      q->oldrsq = q->actual_rsq;
+      double pkp = 0, c_tr = 0, c_tt = 0;
+      for (size_t st = lo; st < hi; st++) {
+        double a = 0, b = 0, c = 0;
+        for (int k = 0; k < 6; k++) {
+          size_t i = 6 * st + k;
+          ttt[i] = ttt[i] + (-msq_x4) * cg_p[i];
+          a += cg_p[i] * ttt[i];
+          b += ttt[i] * res[i];
+          c += ttt[i] * ttt[i];
+        }
+        pkp += a; c_tr += b; c_tt += c;
+      }
+      q->iteration++;
+      double a = -q->rsq / pkp;
+      double actual_rsq = 0;
       for (size_t i = 6 * lo; i < 6 * hi; i++) {
-        ttt[i] = ttt[i] + (-msq_x4) * dest[i];
-        res[i] = src[i] + ttt[i];
-        cg_p[i] = res[i];
-        rsq += res[i] * res[i];
+        dest[i] = dest[i] + a * cg_p[i];
+        res[i] = res[i] + a * ttt[i];
+        actual_rsq += res[i] * res[i];
       }
-      actual_rsq = rsq;
-      if (relrsqmin > 0) relrsq = rel_residue(L, res, dest, parity);
-      final_rsq = rsq / source_norm;
-      final_relrsq = relrsq;
-      iteration++;
-      if (iteration >= max_cg || nrestart >= max_restarts ||
-          ((rsqmin <= 0 || rsqmin > final_rsq) && (relrsqmin <= 0 || relrsqmin > final_relrsq)))
-        break;
-      nrestart++;
+      q->actual_rsq = actual_rsq;
+      q->rsq = q->oldrsq + 2.0 * a * c_tr + a * a * c_tt;
+      if (relrsqmin > 0) q->relrsq = rel_residue(L, res, dest, parity);
+      q->size_r = q->rsq / q->source_norm;
+      q->size_relr = q->relrsq;
+      double b = q->rsq / q->oldrsq;
+      for (size_t i = 6 * lo; i < 6 * hi; i++) cg_p[i] = res[i] + b * cg_p[i];
+      q->mode = 0;
     }
-    oldrsq = actual_rsq;
-    orc_dslash(L, fat, lng, cg_p, ttt, otherparity);
-    orc_dslash(L, fat, lng, ttt, ttt, parity);
-    pkp = 0; c_tr = 0; c_tt = 0;
-    for (size_t s = lo; s < hi; s++) {
-      double a = 0, b = 0, c = 0;
-      for (int k = 0; k < 6; k++) {
-        size_t i = 6 * s + k;
-        ttt[i] = ttt[i] + (-msq_x4) * cg_p[i];
-        a += cg_p[i] * ttt[i];
-        b += ttt[i] * res[i];
-        c += ttt[i] * ttt[i];
+  }
+  for (int s = 0; s < nsrc; s++) {
+    orc_cg_state *q = &S[s];
+    if (q->source_norm != 0.0 && (q->nrestart == max_restarts || q->iteration == max_cg)) q->converged = 0;
+    if (out7) {
+      double *o = out7 + 7 * (size_t)s;
+      if (q->source_norm == 0.0) {
+        for (int k = 0; k < 7; k++) o[k] = 0;
+        o[6] = 1;
+      } else {
+        o[0] = q->final_rsq; o[1] = q->final_relrsq; o[2] = q->size_r; o[3] = q->size_relr;
+        o[4] = q->iteration; o[5] = q->nrestart; o[6] = q->converged;
       }
-      pkp += a; c_tr += b; c_tt += c;
     }
-    iteration++;
-    double a = -rsq / pkp;
-    actual_rsq = 0;
-    for (size_t i = 6 * lo; i < 6 * hi; i++) {
-      dest[i] = dest[i] + a * cg_p[i];
-      res[i] = res[i] + a * ttt[i];
-      actual_rsq += res[i] * res[i];
-    }
-    rsq = oldrsq + 2.0 * a * c_tr + a * a * c_tt;
-    if (relrsqmin > 0) relrsq = rel_residue(L, res, dest, parity);
-    size_r = rsq / source_norm;
-    size_relr = relrsq;
-    double b = rsq / oldrsq;
-    for (size_t i = 6 * lo; i < 6 * hi; i++) cg_p[i] = res[i] + b * cg_p[i];
+    free(q->ttt); free(q->cg_p); free(q->res);
   }
-  if (nrestart == max_restarts || iteration == max_cg) converged = 0;
-  free(ttt); free(cg_p); free(res);
-  if (out) {
-    out[0] = final_rsq; out[1] = final_relrsq; out[2] = size_r; out[3] = size_relr;
-    out[4] = iteration; out[5] = nrestart; out[6] = converged;
-  }
-  return iteration;
+  int maxit = 0;
+  for (int s = 0; s < nsrc; s++) maxit = S[s].iteration > maxit ? S[s].iteration : maxit;
+  free(S); free(vin); free(vout);
+  return maxit;
+}
+
+int orc_congrad(const orc_lat *L, const double *fat, const double *lng,
+                const double *src, double *dest, double mass, int parity,
+                double resid, double relresid, int niter, int max_restarts, double out[7]) {
+  return orc_congrad_multi(L, fat, lng, 1, &src, &dest, mass, parity, resid, relresid, niter, max_restarts, out);
 }
 
 /* ---------------- M^-1: generic_ks/mat_invert.c:18-44,328-407 ---------------- */

@@ -39,6 +39,11 @@ void orc_rephase(const orc_lat *L, double *links);
 
 void orc_dslash(const orc_lat *L, const double *fat, const double *lng,
                 const double *src, double *dst, int parity);
+/* nsrc independent solves in lockstep (one multi-field D per round); each
+   source's result, iteration count and out7[7*s..] equal orc_congrad's */
+int orc_congrad_multi(const orc_lat *L, const double *fat, const double *lng, int nsrc,
+                      const double *const *srcs, double *const *dests, double mass, int parity,
+                      double resid, double relresid, int niter, int max_restarts, double *out7);
 int orc_congrad(const orc_lat *L, const double *fat, const double *lng,
                 const double *src, double *dst, double mass, int parity,
                 double resid, double relresid, int max, int nrestart, double out[7]);

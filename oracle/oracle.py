@@ -38,13 +38,66 @@ def build_oracle():
     subprocess.run(["make", "-s", "-f", os.path.join(HERE, "Makefile")], check=True)
 
 
-def build_ref(ref_root="/root/reference", jobs=8):
-    """Compile MILC's CPU sources into oracle/_ref (only where they exist)."""
-    if not os.path.isdir(ref_root):
-        return False
-    subprocess.run(["make", "-s", "-j%d" % jobs, "-f", os.path.join(HERE, "ref", "Makefile"),
-                    "REF=%s" % ref_root, "OUT=%s" % REF_DIR], check=True)
-    return True
+def build_ref(ref_root=None, jobs=8):
+    """Compile MILC's CPU sources into oracle/_ref with the recipe
+    oracle/ref/Makefile.  ref_root: the reference source tree; by default
+    $MILC_REFERENCE_DIR, else the recipe's own default location.  Where no
+    reference tree exists nothing is built and False is returned."""
+    ref_root = ref_root or os.environ.get("MILC_REFERENCE_DIR")
+    cmd = ["make", "-s", "-j%d" % jobs, "-f", os.path.join(HERE, "ref", "Makefile"), "OUT=%s" % REF_DIR]
+    if ref_root:
+        cmd.append("REF=%s" % ref_root)
+    subprocess.run(cmd, check=True)
+    return ref_available("hisq")
+
+
+def reference_tree():
+    """The reference source tree: $MILC_REFERENCE_DIR, else the tree that
+    oracle/_ref was built from (the recipe records it in oracle/_ref/source_dir),
+    else None (as on hosts without the reference)."""
+    p = os.environ.get("MILC_REFERENCE_DIR")
+    if not p:
+        try:
+            with open(os.path.join(REF_DIR, "source_dir")) as f:
+                p = f.read().strip()
+        except OSError:
+            return None
+    return p if p and os.path.isdir(p) else None
+
+
+# ---- the seeded synthetic inputs (mks_synth.h, compiled into liborc.so) ----
+def _orc_lib():
+    path = os.path.join(HERE, "liborc.so")
+    if not os.path.exists(path):
+        build_oracle()
+    return ctypes.CDLL(path)
+
+
+def _dims_arr(dims):
+    return (ctypes.c_int * 4)(*[int(d) for d in dims])
+
+
+def gen_thin_links(dims, seed, a=0.3):
+    """Unphased thin links U[V][4][18] = exp(i a H); identical to the
+    product library's mks_gen_thin_links (same source)."""
+    U = np.zeros((int(np.prod(dims)), 4, 18))
+    if _orc_lib().orc_gen_thin_links(_dims_arr(dims), ctypes.c_uint64(seed), ctypes.c_double(a), _ptr(U)) != 0:
+        raise ValueError("orc_gen_thin_links: bad dims")
+    return U
+
+
+def gen_vector(dims, seed, parity=EVEN):
+    v = np.zeros((int(np.prod(dims)), 6))
+    if _orc_lib().orc_gen_vector(_dims_arr(dims), ctypes.c_uint64(seed), ctypes.c_int(parity), _ptr(v)) != 0:
+        raise ValueError("orc_gen_vector: bad dims")
+    return v
+
+
+def gen_momenta(dims, seed):
+    m = np.zeros((int(np.prod(dims)), 4, 10))
+    if _orc_lib().orc_gen_momenta(_dims_arr(dims), ctypes.c_uint64(seed), _ptr(m)) != 0:
+        raise ValueError("orc_gen_momenta: bad dims")
+    return m
 
 
 def ref_available(action="hisq"):
@@ -103,6 +156,21 @@ class Oracle:
                                   ctypes.c_double(resid), ctypes.c_double(relresid),
                                   ctypes.c_int(max_iter), ctypes.c_int(nrestart), _ptr(out))
         return it, dst, out
+
+    def congrad_multi(self, fat, lng, srcs, dsts, mass, parity, resid, relresid=0.0, max_iter=1000,
+                      nrestart=5):
+        """Independent CG solves of several sources in lockstep (the links are
+        read once per D for all of them); each result equals congrad's."""
+        n = len(srcs)
+        srcs = [np.ascontiguousarray(s, dtype=np.float64) for s in srcs]
+        dsts = [np.ascontiguousarray(d, dtype=np.float64).copy() for d in dsts]
+        out = np.zeros((n, 7))
+        PA = _dp * n
+        it = self.lib.orc_congrad_multi(self.L, _ptr(fat), _ptr(lng), ctypes.c_int(n), PA(*[_ptr(s) for s in srcs]),
+                                        PA(*[_ptr(d) for d in dsts]), ctypes.c_double(mass), ctypes.c_int(parity),
+                                        ctypes.c_double(resid), ctypes.c_double(relresid),
+                                        ctypes.c_int(max_iter), ctypes.c_int(nrestart), _ptr(out))
+        return it, dsts, out
 
     def mat_invert_uml(self, fat, lng, src, dst, mass, resid, max_iter=1000, nrestart=5):
         dst = dst.copy()

@@ -31,7 +31,7 @@ sys.path.insert(0, HERE)
 
 import scidac  # noqa: E402
 
-DEFAULT = "/root/reference/binary_samples"
+DEFAULT = None  # the reference tree's binary_samples ($MILC_REFERENCE_DIR, or oracle/_ref's source tree)
 NSUB = 512
 
 
@@ -52,6 +52,12 @@ def milc_order(dims):
 
 
 def main(folder=DEFAULT):
+    if not folder:
+        from oracle.oracle import reference_tree
+        ref = reference_tree()
+        if not ref:
+            raise SystemExit("reference tree not found: set MILC_REFERENCE_DIR")
+        folder = os.path.join(ref, "binary_samples")
     lat, info = scidac.read_field(os.path.join(folder, "lat.sample.l8"))
     dims = tuple(info["dims"])
     perm = milc_order(dims)

@@ -24,7 +24,16 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-DEFAULT = "/root/reference"
+def _reference():
+    """The reference tree ($MILC_REFERENCE_DIR, or the one oracle/_ref was built from)."""
+    from oracle.oracle import reference_tree
+    ref = reference_tree()
+    if not ref:
+        raise SystemExit("reference tree not found: set MILC_REFERENCE_DIR")
+    return ref
+
+
+DEFAULT = None
 
 
 def read_milc_lattice(path):
@@ -52,6 +61,7 @@ def read_milc_lattice(path):
 
 
 def main(ref=DEFAULT):
+    ref = ref or _reference()
     from milc_qcd_gb300 import _lib
     from milc_qcd_gb300.rhmc import load_rhmc_params
     dims, lat = read_milc_lattice(os.path.join(ref, "binary_samples", "lat.sample.l6666.hisq"))

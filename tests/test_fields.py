@@ -29,3 +29,15 @@ def test_vector_parity_and_normalisation(lib):
     both = lib.gen_vector(dims, 1, lib.EVENANDODD)
     assert np.array_equal(both[: V // 2], e[: V // 2])
     assert abs(np.mean(both ** 2) - 0.5) < 0.02  # MILC's exp(-x^2) normalisation
+
+
+def test_oracle_generators_equal_product_generators(lib, oracle_cls):
+    """The oracle library compiles the same generator source (mks_synth.h):
+    a process that does not load the product library (the CPU reference arm
+    of the benchmark) builds bit-identical links, sources and momenta."""
+    from oracle import oracle as O
+    dims = (4, 6, 4, 8)
+    assert np.array_equal(O.gen_thin_links(dims, 11, 0.2), lib.gen_thin_links(dims, 11, 0.2))
+    for parity in (lib.EVEN, lib.ODD, lib.EVENANDODD):
+        assert np.array_equal(O.gen_vector(dims, 12, parity), lib.gen_vector(dims, 12, parity))
+    assert np.array_equal(O.gen_momenta(dims, 13), lib.gen_momenta(dims, 13))

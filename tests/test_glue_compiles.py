@@ -7,9 +7,10 @@ import subprocess
 import pytest
 
 from conftest import ROOT
+from oracle.oracle import reference_tree
 
-REF = "/root/reference"
-pytestmark = pytest.mark.skipif(not os.path.isdir(REF), reason="reference tree not present")
+REF = reference_tree() or "<no reference tree>"
+pytestmark = pytest.mark.skipif(reference_tree() is None, reason="reference tree not present")
 
 FLAGS = ["-fsyntax-only", "-std=gnu99", "-w", "-DMILC_PRECISION=2", "-DFN", "-DHMC", "-DHISQ_FF_MULTI_WRAPPER",
          "-DSINGLE", "-DINT_ALG=INT_3G1F", "-DKS_MULTICG=HYBRID", "-DKS_MULTIFF=FNMAT", "-DFEWSUMS",

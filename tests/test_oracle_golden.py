@@ -92,3 +92,27 @@ def test_oracle_asqtad(oracle_cls, asqtad):
     b = asqtad["cg_src"]
     it, x, _ = orc.congrad(fat, lng, b, np.zeros_like(b), float(asqtad["mass"]), 2, 1e-9, 0.0, 40, 10)
     assert it == int(asqtad["cg_iters"]) and rel(x, asqtad["cg_x"]) < 1e-13
+
+
+def test_oracle_lockstep_cg_equals_single_source(oracle_cls, hisq):
+    """The lockstep multi-source oracle CG (used to check the benchmark's block
+    solves at full size) gives each source exactly what the single-source CG
+    gives: solutions bit for bit, same iterations, restarts and residuals.
+    Sources converge at different iterations, one is zero, and the restart
+    length is short so that restarts interleave with the iterations."""
+    from oracle import oracle as O
+    dims = tuple(hisq["dims"])
+    orc = oracle_cls(dims)
+    fat, lng, mass = hisq["fat0"], hisq["lng0"], float(hisq["mass"])
+    srcs = [O.gen_vector(dims, 800 + k, 2) * (1.0 + k) for k in range(3)] + [np.zeros_like(hisq["cg_src"])]
+    srcs[1][::7] *= 30.0  # a differently conditioned right-hand side
+    x0 = [np.zeros_like(s) for s in srcs]
+    x0[2] = O.gen_vector(dims, 900, 2) * 0.1
+    it, xs, out = orc.congrad_multi(fat, lng, srcs, x0, mass, 2, 1e-9, 0.0, 15, 20)
+    its = []
+    for k in range(len(srcs)):
+        itk, xk, ok = orc.congrad(fat, lng, srcs[k], x0[k], mass, 2, 1e-9, 0.0, 15, 20)
+        its.append(itk)
+        assert np.array_equal(xs[k], xk), k
+        assert np.array_equal(out[k], ok), k
+    assert it == max(its) and len(set(its[:3])) > 1
