@@ -333,6 +333,12 @@ int mks_tuned_shape(int prec, int nsrc, int *G, int *nb, int *block);
  * TMA-staged kernel won (then *block = threads per CTA). */
 int mks_tuned_shape_epi(int prec, int nsrc, int *G, int *nb, int *block, int *tma);
 
+/* Which D_eo kernel the tuner chose for (prec, nsrc), plain D (epi = 0) or
+ * fused-epilogue launches (epi = 1): 0 direct loads, 1 TMA-staged links,
+ * 2 direct loads software-pipelined one term deep.  MKS_ERR_STATE when the
+ * pair has not been launched yet. */
+int mks_tuned_variant(int prec, int nsrc, int epi);
+
 /* ------------------------------------------------------------------ */
 /* Gauge side of the RHMC molecular dynamics (mks_gauge.cu).  The library
  * keeps one resident thin-link field (the one the fermion links are built

@@ -115,10 +115,86 @@ struct TileSmem {
   }
 };
 
+// The 16 terms of one output site, links loaded from global memory.
+// PIPE = false: each term loads its link and then applies it.  PIPE = true:
+// a software pipeline one term deep -- the next term's link loads are issued
+// before this term's mat-vecs, so two link fetches from HBM are in flight per
+// thread instead of one (more registers per thread, fewer resident warps).
+template <typename R, class LinkT, class InT, int NB, bool PIPE>
+__device__ __forceinline__ void site_terms(const LinkT &fat, const LinkT &lng, const InT *in, int nsrc, int grp,
+                                           const Geom &g, int par, int h, const int c0[4], V3<R> (&acc)[NB]) {
+  const int Vh = g.Vh, opar = 1 - par;
+  const int L[4] = {g.nx, g.ny, g.nz, g.nt};
+  if constexpr (!PIPE) {
+#pragma unroll
+    for (int mu = 0; mu < 4; mu++) {
+      int hf1, hb1, hf3, hb3;
+      nbr4(g, c0, L, mu, hf1, hb1, hf3, hb3);
+      {
+        const M3<R> U = load_link(fat, par, mu, h, Vh);
+#pragma unroll
+        for (int s = 0; s < NB; s++)
+          if (grp * NB + s < nsrc) mv_acc(U, load_in<LinkT>(in[grp * NB + s], hf1, Vh, fat), acc[s]);
+      }
+      {
+        const M3<R> U = load_link(lng, par, mu, h, Vh);
+#pragma unroll
+        for (int s = 0; s < NB; s++)
+          if (grp * NB + s < nsrc) mv_acc(U, load_in<LinkT>(in[grp * NB + s], hf3, Vh, lng), acc[s]);
+      }
+      {
+        const M3<R> U = load_link(fat, opar, mu, hb1, Vh);
+#pragma unroll
+        for (int s = 0; s < NB; s++)
+          if (grp * NB + s < nsrc) amv_sub(U, load_in<LinkT>(in[grp * NB + s], hb1, Vh, fat), acc[s]);
+      }
+      {
+        const M3<R> U = load_link(lng, opar, mu, hb3, Vh);
+#pragma unroll
+        for (int s = 0; s < NB; s++)
+          if (grp * NB + s < nsrc) amv_sub(U, load_in<LinkT>(in[grp * NB + s], hb3, Vh, lng), acc[s]);
+      }
+    }
+  } else {
+    int hf1, hb1, hf3, hb3;
+    nbr4(g, c0, L, 0, hf1, hb1, hf3, hb3);
+    M3<R> U = load_link(fat, par, 0, h, Vh);
+#pragma unroll
+    for (int mu = 0; mu < 4; mu++) {
+      M3<R> Un = load_link(lng, par, mu, h, Vh);  // next: Naik forward
+#pragma unroll
+      for (int s = 0; s < NB; s++)
+        if (grp * NB + s < nsrc) mv_acc(U, load_in<LinkT>(in[grp * NB + s], hf1, Vh, fat), acc[s]);
+      U = Un;
+      Un = load_link(fat, opar, mu, hb1, Vh);  // next: fat backward
+#pragma unroll
+      for (int s = 0; s < NB; s++)
+        if (grp * NB + s < nsrc) mv_acc(U, load_in<LinkT>(in[grp * NB + s], hf3, Vh, lng), acc[s]);
+      U = Un;
+      Un = load_link(lng, opar, mu, hb3, Vh);  // next: Naik backward
+#pragma unroll
+      for (int s = 0; s < NB; s++)
+        if (grp * NB + s < nsrc) amv_sub(U, load_in<LinkT>(in[grp * NB + s], hb1, Vh, fat), acc[s]);
+      U = Un;
+      int nf1 = 0, nb1 = 0, nf3 = 0, nb3 = 0;
+      if (mu < 3) {
+        nbr4(g, c0, L, mu + 1, nf1, nb1, nf3, nb3);
+        Un = load_link(fat, par, mu + 1, h, Vh);  // next: fat forward of the next direction
+      }
+#pragma unroll
+      for (int s = 0; s < NB; s++)
+        if (grp * NB + s < nsrc) amv_sub(U, load_in<LinkT>(in[grp * NB + s], hb3, Vh, lng), acc[s]);
+      U = Un;
+      hf1 = nf1; hb1 = nb1; hf3 = nf3; hb3 = nb3;
+    }
+  }
+}
+
 // live = false (a TMA tile whose staged links did not arrive): the thread
 // computes and writes nothing but still takes part in the grid reduction
 // with zero sums, so the arrival counters return to zero as in every launch
-template <typename R, class LinkT, class InT, class OutT, int NB, int EPI, int NSUM, class Fin, bool TMA = false>
+template <typename R, class LinkT, class InT, class OutT, int NB, int EPI, int NSUM, class Fin, bool TMA = false,
+          bool PIPE = false>
 __device__ __forceinline__ void dslash_body(const LinkT &fat, const LinkT &lng,
                                             const DslashArgs<InT, OutT, typename EpiLoad<R>::type> &a,
                                             const Fin &fin, const TileSmem ts = TileSmem{nullptr, 0},
@@ -165,6 +241,9 @@ __device__ __forceinline__ void dslash_body(const LinkT &fat, const LinkT &lng,
 #pragma unroll
       for (int c = 0; c < 3; c++) acc[s].c[c] = {R(0), R(0)};
     const int c0[4] = {x, y, z, t};
+    if constexpr (!TMA) {
+      site_terms<R, LinkT, InT, NB, PIPE>(fat, lng, a.in, a.nsrc, grp, g, par, h, c0, acc);
+    } else {
     const int L[4] = {g.nx, g.ny, g.nz, g.nt};
 #pragma unroll
     for (int mu = 0; mu < 4; mu++) {
@@ -215,6 +294,7 @@ __device__ __forceinline__ void dslash_body(const LinkT &fat, const LinkT &lng,
         }
       }
     }
+    }  // TMA
 #pragma unroll
     for (int s = 0; s < NB; s++) {
       const int S = grp * NB + s;
@@ -273,6 +353,20 @@ __global__ void __launch_bounds__(256)
 k_dslash(const LinkT fat, const LinkT lng, const DslashArgs<InT, OutT, typename EpiLoad<R>::type> a,
          const Fin fin) {
   dslash_body<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin>(fat, lng, a, fin);
+}
+
+// the same shapes with the link loads software-pipelined one term deep
+// (site_terms<PIPE = true>); the register allocator is asked for at least
+// MKS_DSLASHP_MINB resident 256-thread blocks per SM (2: up to 128
+// registers per thread), room for the second link in registers
+#ifndef MKS_DSLASHP_MINB
+#define MKS_DSLASHP_MINB 2
+#endif
+template <typename R, class LinkT, class InT, class OutT, int NB, int EPI, int NSUM, class Fin>
+__global__ void __launch_bounds__(256, MKS_DSLASHP_MINB)
+k_dslash_p(const LinkT fat, const LinkT lng, const DslashArgs<InT, OutT, typename EpiLoad<R>::type> a,
+           const Fin fin) {
+  dslash_body<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin, false, true>(fat, lng, a, fin);
 }
 
 // one source, one thread per site (G = NB = 1)

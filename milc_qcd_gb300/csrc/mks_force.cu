@@ -194,28 +194,8 @@ __global__ void __launch_bounds__(128) k_unit_adj(Geom g, const double2 *Vl, con
   MatT<S> Kw = link_dir((T2 *)KW, mu, Vh), Kv = link_dir(KV, mu, Vh);
   const M3<S> V = from64<S>(Vm.ld(par, h, Vh));
   M3<S> Q = tan_<S>(V, V), Q2 = tnn<S>(Q, Q);
-  S c0 = Q.e[0][0].re + Q.e[1][1].re + Q.e[2][2].re;
-  S c1 = (Q2.e[0][0].re + Q2.e[1][1].re + Q2.e[2][2].re) / 2;
-  S q3 = 0;
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int k = 0; k < 3; k++) q3 += Q2.e[i][k].re * Q.e[k][i].re - Q2.e[i][k].im * Q.e[k][i].im;
-  S c2 = q3 / 3, gv[3];
-  S Sv = c1 / 3 - c0 * (c0 / 18);
-  if (fabs(Sv) < (S)1.0e-14) {
-    gv[0] = gv[1] = gv[2] = c0 / 3;
-  } else {
-    S Rr = c2 / 2 - c0 * (c1 / 3) + c0 * c0 * (c0 / 27);
-    Sv = sqrt(Sv);
-    S RoS = Rr / (Sv * Sv * Sv), theta;
-    if (!(fabs(RoS) < (S)1)) theta = Rr > 0 ? (S)0 : (S)3.14159265358979323846264338328;
-    else theta = acos(RoS);
-    S th3 = theta / 3, pi23 = (S)(6.28318530717958647692528676656 / 3);
-    gv[0] = c0 / 3 + 2 * Sv * cos(th3);
-    gv[1] = c0 / 3 + 2 * Sv * cos(th3 + pi23);
-    gv[2] = c0 / 3 + 2 * Sv * cos(th3 + 2 * pi23);
-  }
+  S gv[3];
+  herm3_eigvals<S>(Q, Q2, gv);
   S gmin = fmin(gv[0], fmin(gv[1], gv[2]));
   if (gmin < (S)5.0e-5) {  // HISQ_FORCE_FILTER
     if (nfilter) atomicAdd(nfilter, 1u);

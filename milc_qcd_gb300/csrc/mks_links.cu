@@ -15,9 +15,9 @@
 // per launch (generic/general_staple.c:42-140).  FP64 fields and
 // arithmetic, except in the molecular-dynamics FP32 setting
 // (mks_md_precision): there the thin links are copied to FP32 and every
-// smearing stage is stored and multiplied in FP32; the U(3) projection keeps
-// FP64 arithmetic, and the resident V, W and the slots' fat / long links
-// stay FP64 fields (holding the FP32 results).
+// smearing stage, the U(3) projection included, is stored and computed in
+// FP32, while the resident V, W and the slots' fat / long links stay FP64
+// fields (holding the FP32 results).
 //
 // All link fields use the SoA layout of mks_internal.cuh: [par][dir][9][Vh].
 #include <cmath>
@@ -74,29 +74,9 @@ __global__ void __launch_bounds__(128) k_naik(Geom g, const typename Stor<R>::t 
 template <typename A>
 __device__ void u3_unitarize(const M3<A> &V, M3<A> &W, unsigned int *nsvd) {
   M3<A> Q = tan_<A>(V, V), Q2 = tnn<A>(Q, Q);
-  A c0 = Q.e[0][0].re + Q.e[1][1].re + Q.e[2][2].re;
-  A c1 = (Q2.e[0][0].re + Q2.e[1][1].re + Q2.e[2][2].re) / 2;
-  A q3 = 0;
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int k = 0; k < 3; k++) q3 += Q2.e[i][k].re * Q.e[k][i].re - Q2.e[i][k].im * Q.e[k][i].im;
-  A c2 = q3 / 3;
-  A g0, g1, g2;
-  A S = c1 / 3 - c0 * (c0 / 18);
-  if (fabs(S) < (A)1.0e-14) {
-    g0 = g1 = g2 = c0 / 3;
-  } else {
-    A R = c2 / 2 - c0 * (c1 / 3) + c0 * c0 * (c0 / 27);
-    S = sqrt(S);
-    A RoS = R / (S * S * S), theta;
-    if (!(fabs(RoS) < (A)1)) theta = R > 0 ? (A)0 : (A)3.14159265358979323846264338328;
-    else theta = acos(RoS);
-    A th3 = theta / 3, pi23 = (A)(6.28318530717958647692528676656 / 3);
-    g0 = c0 / 3 + 2 * S * cos(th3);
-    g1 = c0 / 3 + 2 * S * cos(th3 + pi23);
-    g2 = c0 / 3 + 2 * S * cos(th3 + 2 * pi23);
-  }
+  A gv[3];
+  herm3_eigvals<A>(Q, Q2, gv);
+  const A g0 = gv[0], g1 = gv[1], g2 = gv[2];
   // det V for the SVD criterion (FP64 constructions only: the 1e-8 relative
   // test is below FP32 resolution)
   if (sizeof(A) == 8) {

@@ -358,8 +358,9 @@ static LinkSet16 links16(const LinkSlot &s) {
 // mks_tuned_shape().
 // launch shape: G threads per site, NB sources per thread, block size;
 // tma = 1: the FP32 kernel that stages each tile's links in shared memory
-// (NB = 1, block = T G for a tile of T sites)
-struct Shape { int G, NB, block, tma; };
+// (NB = 1, block = T G for a tile of T sites); pipe = 1: the kernel whose
+// link loads are software-pipelined one term deep (k_dslash_p)
+struct Shape { int G, NB, block, tma, pipe; };
 static Shape g_shape[3][MAXSRC + 1];      // [prec][nsrc], G == 0: not chosen yet
 static Shape g_shape_epi[3][MAXSRC + 1];  // the same for the fused-epilogue launches
 static void shapes_reset() {
@@ -378,7 +379,7 @@ void tma_disable() {
   for (auto *tab : {g_shape, g_shape_epi})
     for (int p = 0; p < 3; p++)
       for (int n = 0; n <= MAXSRC; n++)
-        if (tab[p][n].tma) tab[p][n] = Shape{0, 0, 0, 0};
+        if (tab[p][n].tma) tab[p][n] = Shape{0, 0, 0, 0, 0};
   graphs_free_all();
 }
 // true once after tma_disable: the failed call may be repeated
@@ -389,11 +390,11 @@ static bool take_tma_retry() {
 }
 
 static Shape default_shape(int nsrc) {
-  if (nsrc <= 1) return {1, 1, 256, 0};
-  if (nsrc <= 2) return {1, 2, 256, 0};
-  if (nsrc <= 4) return {1, 4, 256, 0};
-  if (nsrc <= 8) return {2, 4, 256, 0};
-  return {4, 4, 256, 0};
+  if (nsrc <= 1) return {1, 1, 256, 0, 0};
+  if (nsrc <= 2) return {1, 2, 256, 0, 0};
+  if (nsrc <= 4) return {1, 4, 256, 0, 0};
+  if (nsrc <= 8) return {2, 4, 256, 0, 0};
+  return {4, 4, 256, 0, 0};
 }
 
 // tile of the TMA kernel for G threads per site: R complete x-rows of nx/2
@@ -422,7 +423,8 @@ template <> struct PrecOf<LinkF16> { enum { v = MKS_PREC_HALF }; typedef VecF16 
 
 template <typename R, class LinkT, class InT, class OutT, int NB, int EPI, int NSUM, class Fin>
 static int launch_dslash_nb(int family, const LinkT &fat, const LinkT &lng,
-                            DslashArgs<InT, OutT, typename EpiLoad<R>::type> &a, const Fin &fin, int block) {
+                            DslashArgs<InT, OutT, typename EpiLoad<R>::type> &a, const Fin &fin, int block,
+                            bool pipe) {
   Context &c = ctx();
   size_t threads = (size_t)c.Vh * a.groups;
   int grid = (int)((threads + block - 1) / block);
@@ -431,7 +433,9 @@ static int launch_dslash_nb(int family, const LinkT &fat, const LinkT &lng,
     a.red = c.red;
   }
   timing_begin(family);
-  if (NB == 1 && a.groups == 1 && block == 256)
+  if (pipe)
+    k_dslash_p<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin><<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
+  else if (NB == 1 && a.groups == 1 && block == 256)
     k_dslash1<R, LinkT, InT, OutT, EPI, NSUM, Fin><<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
   else
     k_dslash<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin><<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
@@ -469,11 +473,12 @@ static int launch_shape(int family, const LinkT &fat, const LinkT &lng,
       return MKS_OK;
     }
   }
+  const bool pipe = sh.pipe != 0;
   switch (sh.NB) {
-  case 1: return launch_dslash_nb<R, LinkT, InT, OutT, 1, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block);
-  case 2: return launch_dslash_nb<R, LinkT, InT, OutT, 2, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block);
-  case 4: return launch_dslash_nb<R, LinkT, InT, OutT, 4, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block);
-  default: return launch_dslash_nb<R, LinkT, InT, OutT, 8, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block);
+  case 1: return launch_dslash_nb<R, LinkT, InT, OutT, 1, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block, pipe);
+  case 2: return launch_dslash_nb<R, LinkT, InT, OutT, 2, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block, pipe);
+  case 4: return launch_dslash_nb<R, LinkT, InT, OutT, 4, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block, pipe);
+  default: return launch_dslash_nb<R, LinkT, InT, OutT, 8, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block, pipe);
   }
 }
 
@@ -486,6 +491,16 @@ static bool tuning_enabled() {
   static int v = -1;
   if (v < 0) {
     const char *e = getenv("MKS_TUNE");
+    v = e ? atoi(e) : 1;
+  }
+  return v != 0;
+}
+
+// MKS_PIPE=0 keeps the software-pipelined D_eo kernel out of the tuner's candidates
+static bool pipe_enabled() {
+  static int v = -1;
+  if (v < 0) {
+    const char *e = getenv("MKS_PIPE");
     v = e ? atoi(e) : 1;
   }
   return v != 0;
@@ -546,8 +561,10 @@ static int tune_shape(const LinkT &fat, const LinkT &lng, int nsrc, Shape *best)
     for (int G = 1; G <= 16; G *= 2) {
       const int NB = nbs[ib];
       if (G * NB < nsrc || G * NB > MAXSRC || (G * NB >= 2 * nsrc && G * NB > 1)) continue;
-      for (int block = 128; block <= 256; block *= 2) {
-        Shape sh = {G, NB, block, 0};
+      for (int cand = 0; cand < 4; cand++) {
+        const int block = (cand & 1) ? 256 : 128, pipe = cand >> 1;
+        if (pipe && !pipe_enabled()) continue;
+        Shape sh = {G, NB, block, 0, pipe};
         float tot = 0;
         for (int it = 0; it < 4; it++) {
           MKS_CUDA(cudaEventRecord(e0, c.stream));
@@ -608,7 +625,9 @@ static bool shape_override(int prec, int nsrc, Shape *out) {
     if (sscanf(item.c_str(), "%d:%d:%d:%d:%d", &p, &n, &G, &NB, &B) == 5 && p == prec &&
         n == nsrc && G >= 1 && G <= 16 && (G & (G - 1)) == 0 && (NB == 1 || NB == 2 || NB == 4 || NB == 8) &&
         G * NB >= nsrc && G * NB <= MAXSRC && (B == 128 || B == 256)) {
-      *out = {G, NB, B, 0};
+      // a trailing ":p" selects the software-pipelined kernel
+      const int pipe = item.size() > 2 && item.compare(item.size() - 2, 2, ":p") == 0;
+      *out = {G, NB, B, 0, pipe};
       return true;
     }
     int T, Rr;
@@ -2477,4 +2496,11 @@ extern "C" int mks_tuned_shape_epi(int prec, int nsrc, int *G, int *nb, int *blo
   if (block) *block = s.block;
   if (tma) *tma = s.tma;
   return MKS_OK;
+}
+
+extern "C" int mks_tuned_variant(int prec, int nsrc, int epi) {
+  if (prec < 0 || prec > 2 || nsrc < 1 || nsrc > MAXSRC) return MKS_ERR_ARG;
+  const Shape &s = (epi ? g_shape_epi : g_shape)[prec][nsrc];
+  if (s.G == 0) return MKS_ERR_STATE;
+  return s.tma ? 1 : (s.pipe ? 2 : 0);
 }

@@ -180,6 +180,37 @@ __device__ __forceinline__ void tacc(M3<R> &d, const M3<R> &s, R f) {
     for (int j = 0; j < 3; j++) { d.e[i][j].re = fma(f, s.e[i][j].re, d.e[i][j].re); d.e[i][j].im = fma(f, s.e[i][j].im, d.e[i][j].im); }
 }
 
+// Eigenvalues g[0..2] of the Hermitian, non-negative Q = V^dag V (Q2 = Q Q)
+// from its invariants c0 = tr Q, c1 = tr Q^2 / 2, c2 = tr Q^3 / 3 by the
+// trigonometric solution of the characteristic cubic -- the first step of
+// the analytic U(3) projection W = V Q^(-1/2) (generic_ks/su3_mat_op.c:
+// 828-1000) and of its adjoint in the fermion force.  Arithmetic A.
+template <typename A>
+__device__ __forceinline__ void herm3_eigvals(const M3<A> &Q, const M3<A> &Q2, A g[3]) {
+  A c0 = Q.e[0][0].re + Q.e[1][1].re + Q.e[2][2].re;
+  A c1 = (Q2.e[0][0].re + Q2.e[1][1].re + Q2.e[2][2].re) / 2;
+  A q3 = 0;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int k = 0; k < 3; k++) q3 += Q2.e[i][k].re * Q.e[k][i].re - Q2.e[i][k].im * Q.e[k][i].im;
+  A c2 = q3 / 3;
+  A S = c1 / 3 - c0 * (c0 / 18);
+  if (fabs(S) < (A)1.0e-14) {
+    g[0] = g[1] = g[2] = c0 / 3;
+  } else {
+    A R = c2 / 2 - c0 * (c1 / 3) + c0 * c0 * (c0 / 27);
+    S = sqrt(S);
+    A RoS = R / (S * S * S), theta;
+    if (!(fabs(RoS) < (A)1)) theta = R > 0 ? (A)0 : (A)3.14159265358979323846264338328;
+    else theta = acos(RoS);
+    A th3 = theta / 3, pi23 = (A)(6.28318530717958647692528676656 / 3);
+    g[0] = c0 / 3 + 2 * S * cos(th3);
+    g[1] = c0 / 3 + 2 * S * cos(th3 + pi23);
+    g[2] = c0 / 3 + 2 * S * cos(th3 + 2 * pi23);
+  }
+}
+
 // neighbour (checkerboard index) of site (par,h) displaced by d along mu
 __device__ __forceinline__ int nbr(const Geom &g, int par, int h, int mu, int d) {
   int c[4];

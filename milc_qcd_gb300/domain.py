@@ -12,33 +12,28 @@ from the neighbouring ranks; the results on the interior sites equal those
 of the global operator exactly, because every site's arithmetic is the
 same.  A CG over the decomposition adds one global sum per dot product.
 
-This module holds the index maps and the pack / exchange / unpack steps;
-the exchange itself goes through torch.distributed point-to-point calls
-(NCCL between GPUs, gloo between CPU ranks), or a direct copy when both
-sub-domains live in one process.
+This module holds the index maps and the pack / exchange / unpack steps on
+host (numpy) fields; the exchange itself goes through torch.distributed
+point-to-point calls, or a direct copy when both sub-domains live in one
+process.  Faces are packed and unpacked on the host; with the NCCL backend
+(one GPU per rank) they travel as device tensors, with gloo as host tensors.
 """
-import ctypes
-
 import numpy as np
 
 GHOST = 4
 
 
 def _site_index_table(dims):
-    """MILC index of every site, as a lexicographic (t, z, y, x) array."""
-    from . import _lib
-    lib = _lib.load()
-    d4 = (ctypes.c_int * 4)(*dims)
+    """MILC index of every site, as a lexicographic (t, z, y, x) array:
+    lexicographic i = x + nx (y + ny (z + nz t)); even sites (x+y+z+t even)
+    at i/2, odd sites at (i + V)/2 (generic/layout_hyper_prime.c:509-520,
+    the same map as mks_site_index)."""
     nx, ny, nz, nt = dims
-    out = np.zeros((nt, nz, ny, nx), dtype=np.int64)
-    c = (ctypes.c_int * 4)()
-    for t in range(nt):
-        for z in range(nz):
-            for y in range(ny):
-                for x in range(nx):
-                    c[0], c[1], c[2], c[3] = x, y, z, t
-                    out[t, z, y, x] = lib.mks_site_index(d4, c)
-    return out
+    V = nx * ny * nz * nt
+    t, z, y, x = np.meshgrid(np.arange(nt), np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    i = x + nx * (y + ny * (z + nz * t))
+    odd = ((x + y + z + t) & 1).astype(bool)
+    return np.where(odd, (i + V) // 2, i // 2).astype(np.int64)
 
 
 class TSlabs:
@@ -113,18 +108,21 @@ class TSlabs:
         return locals_
 
     def exchange_dist(self, local, rank):
-        """Halo exchange with torch.distributed (one rank per sub-domain)."""
+        """Halo exchange with torch.distributed (one rank per sub-domain).
+        The faces travel as tensors on the backend's device: CUDA tensors for
+        NCCL (which carries device memory only), host tensors for gloo."""
         import torch
         import torch.distributed as dist
         R = self.R
+        dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
         up, down = self.face_send(local, +1), self.face_send(local, -1)
-        recv_lo, recv_hi = np.empty_like(up), np.empty_like(down)
-        t_up, t_down = torch.from_numpy(np.ascontiguousarray(up)), torch.from_numpy(np.ascontiguousarray(down))
-        t_lo, t_hi = torch.from_numpy(recv_lo), torch.from_numpy(recv_hi)
+        t_up = torch.from_numpy(np.ascontiguousarray(up)).to(dev)
+        t_down = torch.from_numpy(np.ascontiguousarray(down)).to(dev)
+        t_lo, t_hi = torch.empty_like(t_up), torch.empty_like(t_down)
         ops = [dist.P2POp(dist.isend, t_up, (rank + 1) % R), dist.P2POp(dist.irecv, t_lo, (rank - 1) % R),
                dist.P2POp(dist.isend, t_down, (rank - 1) % R), dist.P2POp(dist.irecv, t_hi, (rank + 1) % R)]
         for req in dist.batch_isend_irecv(ops):
             req.wait()
-        self.face_recv(local, -1, recv_lo)
-        self.face_recv(local, +1, recv_hi)
+        self.face_recv(local, -1, t_lo.cpu().numpy())
+        self.face_recv(local, +1, t_hi.cpu().numpy())
         return local

@@ -147,3 +147,19 @@ def test_two_subdomains_on_one_gpu(gpu, oracle_cls):
         d = m.dslash_fn_field(locs["src"][r], np.zeros_like(locs["src"][r]), m.EVENANDODD)
         D.gather_interior(d, r, got)
     assert np.array_equal(got, want)
+
+
+def test_site_index_table_matches_library(lib):
+    """The vectorised MILC site map equals the library's mks_site_index."""
+    import ctypes
+    from milc_qcd_gb300.domain import _site_index_table
+    dims = (4, 6, 2, 8)
+    tab = _site_index_table(dims)
+    L = lib._lib.load()
+    d4 = (ctypes.c_int * 4)(*dims)
+    for t in range(dims[3]):
+        for z in range(dims[2]):
+            for y in range(dims[1]):
+                for x in range(dims[0]):
+                    assert tab[t, z, y, x] == L.mks_site_index(d4, (ctypes.c_int * 4)(x, y, z, t))
+    assert sorted(tab.reshape(-1)) == list(range(int(np.prod(dims))))

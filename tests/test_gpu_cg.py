@@ -114,6 +114,28 @@ def test_mat_invert_uml_matches_oracle(gpu, oracle_cls, prec):
     assert rel(Mx, src) < 1e-9
 
 
+@pytest.mark.parametrize("prec", ["PREC_DOUBLE", "PREC_SINGLE"])
+def test_mat_invert_block_uml_matches_oracle(gpu, oracle_cls, prec):
+    """mat_invert_block_uml (generic_ks/mat_invert.c:409-483): M^-1 of several
+    sources in one call; each solution against the oracle's single-source
+    mat_invert_uml and checked through M x = src with the oracle's D."""
+    m = gpu
+    orc, fat, lng = _setup(m, oracle_cls)
+    nsrc = 5
+    srcs = [m.gen_vector(DIMS, 140 + k, m.EVENANDODD) * (1.0 + 0.5 * k) for k in range(nsrc)]
+    # the even half of dst is the even solve's initial guess (as in MILC); the
+    # odd half is rebuilt from it and polished
+    xs = [np.full_like(s, 0.25) for s in srcs]
+    qic = m.QuarkInvertControl(resid=1e-10, max=1000, nrestart=5, prec=getattr(m, prec))
+    it = m.mat_invert_block_uml(srcs, xs, qic, 0.05)
+    assert it > 0
+    for k in range(nsrc):
+        _, xo, _ = orc.mat_invert_uml(fat, lng, srcs[k], np.zeros_like(srcs[k]), 0.05, 1e-12)
+        assert rel(xs[k], xo) < 1e-8, (k, rel(xs[k], xo))
+        Mx = 2 * 0.05 * xs[k] + orc.dslash(fat, lng, xs[k], m.EVENANDODD)
+        assert rel(Mx, srcs[k]) < 1e-9, k
+
+
 def test_graph_replay_with_kernel_timing(gpu, oracle_cls):
     """Solver batches replay as CUDA graphs after their first (eager) run;
     with kernel timing on, the replays carry their own event-record nodes and
