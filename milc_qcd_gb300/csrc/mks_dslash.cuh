@@ -357,10 +357,12 @@ k_dslash(const LinkT fat, const LinkT lng, const DslashArgs<InT, OutT, typename 
 
 // the same shapes with the link loads software-pipelined one term deep
 // (site_terms<PIPE = true>); the register allocator is asked for at least
-// MKS_DSLASHP_MINB resident 256-thread blocks per SM (2: up to 128
-// registers per thread), room for the second link in registers
+// MKS_DSLASHP_MINB resident 256-thread blocks per SM (3: up to 80 registers
+// per thread, room for the second link without spills up to 4 sources per
+// thread; with 2 the allocator took 126 registers and the kernel ran 1.5x
+// slower on GB300)
 #ifndef MKS_DSLASHP_MINB
-#define MKS_DSLASHP_MINB 2
+#define MKS_DSLASHP_MINB 3
 #endif
 template <typename R, class LinkT, class InT, class OutT, int NB, int EPI, int NSUM, class Fin>
 __global__ void __launch_bounds__(256, MKS_DSLASHP_MINB)

@@ -611,8 +611,9 @@ static int tune_shape(const LinkT &fat, const LinkT &lng, int nsrc, Shape *best)
 // cache written by the user); entries must satisfy G*NB >= nsrc, G*NB <= 16,
 // NB in {1,2,4,8}, G a power of two, block in {128,256}.  The entry
 // "prec:nsrc:G:1:tma" (prec 1, FP32) selects the TMA-staged kernel with G
-// threads per site, where the lattice admits its tiles.
-static bool shape_override(int prec, int nsrc, Shape *out) {
+// threads per site, where the lattice admits its tiles.  A leading "d" or
+// "e" limits an entry to the plain D or to the fused-epilogue launches.
+static bool shape_override(int prec, int nsrc, bool epi, Shape *out) {
   const char *e = getenv("MKS_SHAPE");
   if (!e) return false;
   std::string str(e);
@@ -620,7 +621,15 @@ static bool shape_override(int prec, int nsrc, Shape *out) {
   while (pos < str.size()) {
     size_t end = str.find(',', pos);
     if (end == std::string::npos) end = str.size();
-    const std::string item = str.substr(pos, end - pos);
+    std::string item = str.substr(pos, end - pos);
+    if (!item.empty() && (item[0] == 'd' || item[0] == 'e')) {
+      const bool for_epi = item[0] == 'e';
+      item = item.substr(1);
+      if (for_epi != epi) {
+        pos = end + 1;
+        continue;
+      }
+    }
     int p, n, G, NB, B;
     if (sscanf(item.c_str(), "%d:%d:%d:%d:%d", &p, &n, &G, &NB, &B) == 5 && p == prec &&
         n == nsrc && G >= 1 && G <= 16 && (G & (G - 1)) == 0 && (NB == 1 || NB == 2 || NB == 4 || NB == 8) &&
@@ -649,7 +658,7 @@ static int launch_dslash(int family, const LinkT &fat, const LinkT &lng,
   Shape &sh = (EPI == EPI_AXPY ? g_shape_epi : g_shape)[pk][a.nsrc];
   if (sh.G == 0) {
     Shape t;
-    if (!shape_override(pk, a.nsrc, &t)) {
+    if (!shape_override(pk, a.nsrc, EPI == EPI_AXPY, &t)) {
       if (EPI == EPI_AXPY) MKS_TRY((tune_shape<LinkT, EPI_AXPY>(fat, lng, a.nsrc, &t)));
       else MKS_TRY(tune_shape(fat, lng, a.nsrc, &t));
     }

@@ -352,3 +352,27 @@ void reunitarize_gpu(void) {
 
 void *qudaAllocatePinned(size_t bytes) { return malloc(bytes); }
 void qudaFreePinned(void *ptr) { free(ptr); }
+
+/* The site links as one su3_matrix[4*sites_on_node] array: what
+ * fermion_links_from_site.c:14-58 asks for under -DUSE_FL_GPU (the QUDA
+ * build takes it from include/generic_quda.h, which needs QUDA). */
+void *create_G_from_site_quda(void) {
+  int i;
+  site *s;
+  su3_matrix *links = (su3_matrix *)qudaAllocatePinned((size_t)sites_on_node * 4 * sizeof(su3_matrix));
+  if (!links) mks_die("create_G_from_site_quda", MKS_ERR_NOMEM);
+  FORALLSITES(i, s) { memcpy(links + 4 * i, s->link, 4 * sizeof(su3_matrix)); }
+  return links;
+}
+void destroy_G_quda(void *links) { qudaFreePinned(links); }
+
+/* The option string MILC prints at start-up (show_generic_ks_md_opts.c:12);
+ * its definition lives in fermion_force_hisq_multi.c, which this binding
+ * replaces (generic_ks/fermion_force_hisq_multi.c:277-293). */
+const char *ks_multiff_opt_chr(void) {
+  switch (KS_MULTIFF) {
+  case ASVEC: return "ASVEC";
+  case FNMATREV: return "FNMATREV";
+  default: return "FNMAT";
+  }
+}
