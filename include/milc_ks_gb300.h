@@ -333,6 +333,15 @@ int mks_tuned_shape(int prec, int nsrc, int *G, int *nb, int *block);
  * TMA-staged kernel won (then *block = threads per CTA). */
 int mks_tuned_shape_epi(int prec, int nsrc, int *G, int *nb, int *block, int *tma);
 
+/* Counts of the last multi-shift call's iteration phase (no counterpart in
+ * the reference; used to state the bytes the multi-shift update kernel
+ * moves): the iterations and the shift updates, i.e. the shifts the update
+ * kernel advanced summed over the iterations (a shift that has converged is
+ * no longer advanced).  Per shift update the kernel moves 4 colour vectors
+ * (psim and pm read and written), per iteration 4 more (r read and written,
+ * ttt read, p written). */
+int mks_multishift_counts(long long *iters, long long *shift_updates);
+
 /* Which D_eo kernel the tuner chose for (prec, nsrc), plain D (epi = 0) or
  * fused-epilogue launches (epi = 1): 0 direct loads, 1 TMA-staged links,
  * 2 direct loads software-pipelined one term deep.  MKS_ERR_STATE when the

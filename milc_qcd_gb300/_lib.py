@@ -111,6 +111,7 @@ SIGNATURES = {
     "mks_tuned_shape": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, IP, IP, IP]),
     "mks_tuned_shape_epi": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, IP, IP, IP, IP]),
     "mks_tuned_variant": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "mks_multishift_counts": (ctypes.c_int, [ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]),
     "mks_site_coords": (None, [IP, ctypes.c_size_t, IP]),
     "mks_site_index": (ctypes.c_size_t, [IP, IP]),
     "mks_staggered_phase": (ctypes.c_double, [IP, IP, ctypes.c_int]),

@@ -1644,6 +1644,7 @@ struct MsState {
   int iter, niter, status, j_low, num_now, num_offsets, need_scroll, want_reliable;
   int n_reliable, pad;
   int retired[MAXSH];
+  long long shift_updates;  // sum over iterations of the shifts the update kernel advanced
 };
 
 // the zeta / beta / alpha recurrences of one field after K2 (t: its three sums)
@@ -1690,6 +1691,8 @@ __device__ __forceinline__ void ms_alpha(MsState &m, const double *t) {
         m.alpha[j] = 0.0;
     }
     if (!isfinite(m.beta_i[jl])) m.status = ST_HOST;
+    // the update kernel of this iteration advances every shift not retired
+    for (int j = 0; j < m.num_now; j++) m.shift_updates += m.retired[j] ? 0 : 1;
 }
 
 struct FinMsAlpha {
@@ -1921,7 +1924,7 @@ static int ms_fold(int nsh, double2 *const *x64, void *const *x32) {
     memset(&op, 0, sizeof op);
     for (int s = 0; s < nb; s++) { op.x64[s] = x64[b0 + s]; op.x32[s] = (float2 *)x32[b0 + s]; }
     op.Vh = (int)ctx().Vh;
-    MKS_TRY((launch_site<OpMsFold, 0, FinNone>(MKS_K_SHIFT, op, FinNone(), nullptr, nb)));
+    MKS_TRY((launch_site<OpMsFold, 0, FinNone>(MKS_K_BLAS, op, FinNone(), nullptr, nb)));
   }
   return MKS_OK;
 }
@@ -1983,7 +1986,7 @@ static int multishift_core(const LinkSlot &sl, int par, int prec, const double2 
     op.r = r; op.cgp = cgp; op.src = src64; op.p16 = p16; op.p16n = p16n; op.Vh = Vh; op.n = nsh;
     double *tot;
     MKS_TRY(wsv("ms_tot", 4, &tot));
-    MKS_TRY((launch_site<OpShiftInit<R>, 1, FinNone>(MKS_K_SHIFT, op, FinNone(), nullptr, 1, tot)));
+    MKS_TRY((launch_site<OpShiftInit<R>, 1, FinNone>(MKS_K_BLAS, op, FinNone(), nullptr, 1, tot)));
     double sn = 0;
     MKS_CUDA(cudaMemcpyAsync(&sn, tot, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     MKS_CUDA(cudaStreamSynchronize(c.stream));
@@ -2084,7 +2087,7 @@ static int multishift_core(const LinkSlot &sl, int par, int prec, const double2 
       MKS_TRY(apply_DD64(sl, par, 1, &xl, &t64, &dd64));
       OpMsResid op;
       op.src = src64; op.ddx = dd64; op.x = xl; op.r32 = (float2 *)r; op.sigma = offsets[h.j_low]; op.Vh = Vh;
-      MKS_TRY((launch_site<OpMsResid, 1, FinNone>(MKS_K_SHIFT, op, FinNone(), nullptr, 1, tot)));
+      MKS_TRY((launch_site<OpMsResid, 1, FinNone>(MKS_K_BLAS, op, FinNone(), nullptr, 1, tot)));
       double rr = 0;
       MKS_CUDA(cudaMemcpyAsync(&rr, tot, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
       MKS_CUDA(cudaStreamSynchronize(c.stream));
@@ -2154,7 +2157,7 @@ static int multishift_multi_core(const LinkSlot &sl, int par, int nf, const doub
     memset(&op, 0, sizeof op);
     for (int j = 0; j < nsh[f]; j++) { op.psim[j] = psim[f][j]; op.pm[j] = pm[f][j]; }
     op.r = r[f]; op.cgp = cgp[f]; op.src = src64[f]; op.Vh = Vh; op.n = nsh[f];
-    MKS_TRY((launch_site<OpShiftInit<float>, 1, FinNone>(MKS_K_SHIFT, op, FinNone(), nullptr, 1, tot1)));
+    MKS_TRY((launch_site<OpShiftInit<float>, 1, FinNone>(MKS_K_BLAS, op, FinNone(), nullptr, 1, tot1)));
     double sn = 0;
     MKS_CUDA(cudaMemcpyAsync(&sn, tot1, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     MKS_CUDA(cudaStreamSynchronize(c.stream));
@@ -2248,7 +2251,7 @@ static int multishift_multi_core(const LinkSlot &sl, int par, int nf, const doub
       MKS_TRY(apply_DD64(sl, par, 1, &xl, &t64, &dd64));
       OpMsResid op;
       op.src = src64[f]; op.ddx = dd64; op.x = xl; op.r32 = r[f]; op.sigma = offsets[f][h.j_low]; op.Vh = Vh;
-      MKS_TRY((launch_site<OpMsResid, 1, FinNone>(MKS_K_SHIFT, op, FinNone(), nullptr, 1, tot1)));
+      MKS_TRY((launch_site<OpMsResid, 1, FinNone>(MKS_K_BLAS, op, FinNone(), nullptr, 1, tot1)));
       double rr = 0;
       MKS_CUDA(cudaMemcpyAsync(&rr, tot1, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
       MKS_CUDA(cudaStreamSynchronize(c.stream));
@@ -2297,6 +2300,12 @@ static int multishift_multi_dev_once(int nf, const double *const *src_dev, const
   MsState hs[MSF];
   MKS_TRY(multishift_multi_core(sl, par, nf, src64, num_offsets, offs, arg->resid, arg->max * arg->nrestart, x64p,
                                 arg->delta > 0 ? arg->delta : 0.1, hs));
+  g_ms_iters = 0;
+  g_ms_shift_updates = 0;
+  for (int f = 0; f < nf; f++) {
+    g_ms_iters = hs[f].iter > g_ms_iters ? hs[f].iter : g_ms_iters;
+    g_ms_shift_updates += hs[f].shift_updates;
+  }
   // FP64 check of every shift of every field, refinement of those that miss
   // (ks_multicg.c:170-228), blocks of up to MAXSRC shifts across the fields
   const int total = base[nf];
@@ -2345,6 +2354,8 @@ static int multishift_dev_once(const double *src_dev, double *const *psim_dev, c
   void *psim[MAXSH];
   if (arg->prec == MKS_PREC_DOUBLE) {
     MKS_TRY(multishift_core<double>(sl, par, MKS_PREC_DOUBLE, src64, nsh, offsets, arg->resid, niter, psim, &h));
+    g_ms_iters = h.iter;
+    g_ms_shift_updates = h.shift_updates;
     for (int j = 0; j < nsh; j++) {
       MKS_TRY(vec_soa64_to_aos((double2 *)psim[j], psim_dev[j], par));
       res[j] = mks_invert_result();
@@ -2368,6 +2379,8 @@ static int multishift_dev_once(const double *src_dev, double *const *psim_dev, c
   MKS_TRY(multishift_core<float>(sl, par, arg->prec, src64, nsh, offsets, arg->resid, niter, psim, &h, x64,
                                  arg->delta > 0 ? arg->delta : 0.1));
   int total_iters = h.iter;
+  g_ms_iters = h.iter;
+  g_ms_shift_updates = h.shift_updates;
   for (int b0 = 0; b0 < nsh; b0 += MAXSRC) {
     int nb = nsh - b0 < MAXSRC ? nsh - b0 : MAXSRC;
     CgFields f;
@@ -2400,6 +2413,10 @@ static int multishift_dev(const double *src_dev, double *const *psim_dev, const 
   if (rc == MKS_ERR_TIMEOUT && take_tma_retry()) rc = multishift_dev_once(src_dev, psim_dev, offsets, nsh, slot, arg, res);
   return rc;
 }
+// iterations and shift updates (shifts advanced, summed over iterations) of
+// the last multi-shift iteration phase, for the update kernel's byte count
+static long long g_ms_iters = 0, g_ms_shift_updates = 0;
+
 static int multishift_multi_dev(int nf, const double *const *src_dev, const int *num_offsets, const double *offsets,
                                 double *const *psim_dev, int slot, const mks_invert_arg *arg, mks_invert_result *res) {
   int rc = multishift_multi_dev_once(nf, src_dev, num_offsets, offsets, psim_dev, slot, arg, res);
@@ -2504,6 +2521,12 @@ extern "C" int mks_tuned_shape_epi(int prec, int nsrc, int *G, int *nb, int *blo
   if (nb) *nb = s.NB;
   if (block) *block = s.block;
   if (tma) *tma = s.tma;
+  return MKS_OK;
+}
+
+extern "C" int mks_multishift_counts(long long *iters, long long *shift_updates) {
+  if (iters) *iters = g_ms_iters;
+  if (shift_updates) *shift_updates = g_ms_shift_updates;
   return MKS_OK;
 }
 

@@ -140,3 +140,31 @@ def test_multishift_page_locked_host_arrays(gpu, oracle_cls):
         assert per[j].converged == 1
         assert np.array_equal(pp[j], ref[j]), j
         assert np.all(pp[j][V2:] == 0.25)
+
+
+def test_multishift_counts_bound_the_update_work(gpu, oracle_cls):
+    """mks_multishift_counts reports the iteration phase's iterations and
+    shift updates: every iteration advances the lowest shift and at most all
+    of them; in mixed precision, shifts converged a decade below the target
+    stop being advanced before the end."""
+    import ctypes
+    m = gpu
+    U, orc, L = hisq_setup(m, oracle_cls, DIMS)
+    m.set_lattice(DIMS)
+    m.load_fn_links(L["fat"][0], L["lng"][0])
+    b = m.gen_vector(DIMS, 57, m.EVEN)
+    offs = 4 * 0.02 ** 2 + np.logspace(-4, 0, 11)
+    lib = m._lib.load()
+    n_it, n_upd = ctypes.c_longlong(), ctypes.c_longlong()
+    psim = [np.zeros_like(b) for _ in offs]
+    qic = m.QuarkInvertControl(resid=1e-10, max=1000, nrestart=5, parity=m.EVEN, prec=m.PREC_DOUBLE)
+    it, _ = m.ks_multicg_offset_field(b, psim, offs, qic)
+    m.check(lib.mks_multishift_counts(ctypes.byref(n_it), ctypes.byref(n_upd)), "counts")
+    assert n_it.value == it
+    assert n_it.value <= n_upd.value <= len(offs) * n_it.value
+    psim = [np.zeros_like(b) for _ in offs]
+    qic = m.QuarkInvertControl(resid=1e-10, max=1000, nrestart=5, parity=m.EVEN, prec=m.PREC_SINGLE)
+    it, _ = m.ks_multicg_offset_field(b, psim, offs, qic)
+    m.check(lib.mks_multishift_counts(ctypes.byref(n_it), ctypes.byref(n_upd)), "counts")
+    assert 0 < n_it.value <= it  # `it` also counts the refinement iterations
+    assert n_it.value <= n_upd.value < len(offs) * n_it.value
