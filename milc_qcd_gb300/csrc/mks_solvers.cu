@@ -2271,6 +2271,10 @@ static int multishift_multi_core(const LinkSlot &sl, int par, int nf, const doub
 
 // nf fields on one slot: offsets, psim_dev and res are the fields' lists one
 // after the other (num_offsets[f] entries each)
+// iterations and shift updates (shifts advanced, summed over iterations) of
+// the last multi-shift iteration phase, for the update kernel's byte count
+static long long g_ms_iters = 0, g_ms_shift_updates = 0;
+
 static int multishift_multi_dev_once(int nf, const double *const *src_dev, const int *num_offsets,
                                      const double *offsets, double *const *psim_dev, int slot,
                                      const mks_invert_arg *arg, mks_invert_result *res) {
@@ -2413,10 +2417,6 @@ static int multishift_dev(const double *src_dev, double *const *psim_dev, const 
   if (rc == MKS_ERR_TIMEOUT && take_tma_retry()) rc = multishift_dev_once(src_dev, psim_dev, offsets, nsh, slot, arg, res);
   return rc;
 }
-// iterations and shift updates (shifts advanced, summed over iterations) of
-// the last multi-shift iteration phase, for the update kernel's byte count
-static long long g_ms_iters = 0, g_ms_shift_updates = 0;
-
 static int multishift_multi_dev(int nf, const double *const *src_dev, const int *num_offsets, const double *offsets,
                                 double *const *psim_dev, int slot, const mks_invert_arg *arg, mks_invert_result *res) {
   int rc = multishift_multi_dev_once(nf, src_dev, num_offsets, offsets, psim_dev, slot, arg, res);
