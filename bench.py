@@ -428,14 +428,18 @@ def gpu_arm(args):
     # launch shapes the autotuner chose for the sloppy D_eo of this solve
     shapes = {}
     G, nb, blk, tma = (ctypes.c_int() for _ in range(4))
-    variants = {0: "direct loads", 1: "TMA-staged links", 2: "direct loads, pipelined"}
+    def variant(v):
+        if v is None or v < 0:
+            return None
+        return ["direct loads", "TMA-staged links", "direct loads, pipelined"][v & 3] + \
+            (", persistent grid" if v & 4 else "")
     if lib.mks_tuned_shape(prec, N, ctypes.byref(G), ctypes.byref(nb), ctypes.byref(blk)) == 0:
         shapes["D"] = {"G": G.value, "NB": nb.value, "block": blk.value,
-                       "kernel": variants.get(lib.mks_tuned_variant(prec, N, 0))}
+                       "kernel": variant(lib.mks_tuned_variant(prec, N, 0))}
     if lib.mks_tuned_shape_epi(prec, N, ctypes.byref(G), ctypes.byref(nb), ctypes.byref(blk),
                                ctypes.byref(tma)) == 0:
         shapes["D+epilogue"] = {"G": G.value, "NB": nb.value, "block": blk.value, "tma": tma.value,
-                                "kernel": variants.get(lib.mks_tuned_variant(prec, N, 1))}
+                                "kernel": variant(lib.mks_tuned_variant(prec, N, 1))}
     dslash_ms = tot_ms.value / max(nl.value, 1)
     Vh = V // 2
     if prec == m.PREC_HALF:

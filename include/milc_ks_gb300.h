@@ -344,8 +344,9 @@ int mks_multishift_counts(long long *iters, long long *shift_updates);
 
 /* Which D_eo kernel the tuner chose for (prec, nsrc), plain D (epi = 0) or
  * fused-epilogue launches (epi = 1): 0 direct loads, 1 TMA-staged links,
- * 2 direct loads software-pipelined one term deep.  MKS_ERR_STATE when the
- * pair has not been launched yet. */
+ * 2 direct loads software-pipelined one term deep; plus 4 when the launch
+ * uses a persistent grid (the CTAs that fit at once loop over the sites).
+ * MKS_ERR_STATE when the pair has not been launched yet. */
 int mks_tuned_variant(int prec, int nsrc, int epi);
 
 /* ------------------------------------------------------------------ */

@@ -360,7 +360,10 @@ static LinkSet16 links16(const LinkSlot &s) {
 // tma = 1: the FP32 kernel that stages each tile's links in shared memory
 // (NB = 1, block = T G for a tile of T sites); pipe = 1: the kernel whose
 // link loads are software-pipelined one term deep (k_dslash_p)
-struct Shape { int G, NB, block, tma, pipe; };
+// persist = 1: a persistent grid (as many CTAs as fit on the GPU at once)
+// that loops over the site blocks, so a fused-epilogue launch reduces its
+// dot products once per CTA rather than once per site block
+struct Shape { int G, NB, block, tma, pipe, persist; };
 static Shape g_shape[3][MAXSRC + 1];      // [prec][nsrc], G == 0: not chosen yet
 static Shape g_shape_epi[3][MAXSRC + 1];  // the same for the fused-epilogue launches
 static void shapes_reset() {
@@ -379,7 +382,7 @@ void tma_disable() {
   for (auto *tab : {g_shape, g_shape_epi})
     for (int p = 0; p < 3; p++)
       for (int n = 0; n <= MAXSRC; n++)
-        if (tab[p][n].tma) tab[p][n] = Shape{0, 0, 0, 0, 0};
+        if (tab[p][n].tma) tab[p][n] = Shape{0, 0, 0, 0, 0, 0};
   graphs_free_all();
 }
 // true once after tma_disable: the failed call may be repeated
@@ -421,24 +424,53 @@ template <> struct PrecOf<LinkF64> { enum { v = MKS_PREC_DOUBLE }; typedef VecF6
 template <> struct PrecOf<LinkF32> { enum { v = MKS_PREC_SINGLE }; typedef VecF32 In; typedef VecF32 Out; typedef float R; };
 template <> struct PrecOf<LinkF16> { enum { v = MKS_PREC_HALF }; typedef VecF16 In; typedef VecF32 Out; typedef float R; };
 
+// CTAs of `kernel` with `block` threads that fit on one SM at once
+template <class K> static int resident_blocks(K kernel, int block) {
+  static std::map<std::pair<const void *, int>, int> cache;
+  const auto key = std::make_pair((const void *)kernel, block);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, block, 0) != cudaSuccess || n < 1) {
+    cudaGetLastError();
+    n = 1;
+  }
+  cache[key] = n;
+  return n;
+}
+
 template <typename R, class LinkT, class InT, class OutT, int NB, int EPI, int NSUM, class Fin>
 static int launch_dslash_nb(int family, const LinkT &fat, const LinkT &lng,
                             DslashArgs<InT, OutT, typename EpiLoad<R>::type> &a, const Fin &fin, int block,
-                            bool pipe) {
+                            bool pipe, bool persist) {
   Context &c = ctx();
   size_t threads = (size_t)c.Vh * a.groups;
-  int grid = (int)((threads + block - 1) / block);
+  const int nvb = (int)((threads + block - 1) / block);
+  auto kp = k_dslash_p<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin>;
+  auto k1 = k_dslash1<R, LinkT, InT, OutT, EPI, NSUM, Fin>;
+  auto kd = k_dslash<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin>;
+  const bool one = !pipe && NB == 1 && a.groups == 1 && block == 256;
+  int grid = nvb;
+  a.nvb = 0;
+  if (persist) {
+    const int nres = pipe ? resident_blocks(kp, block) : (one ? resident_blocks(k1, block) : resident_blocks(kd, block));
+    const int cap = nres * c.sm_count;
+    if (cap < nvb) {
+      grid = cap;
+      a.nvb = nvb;
+    }
+  }
   if (NSUM > 0) {
     MKS_TRY(ensure_red(NSUM * a.groups * NB, grid));
     a.red = c.red;
   }
   timing_begin(family);
   if (pipe)
-    k_dslash_p<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin><<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
-  else if (NB == 1 && a.groups == 1 && block == 256)
-    k_dslash1<R, LinkT, InT, OutT, EPI, NSUM, Fin><<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
+    kp<<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
+  else if (one)
+    k1<<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
   else
-    k_dslash<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin><<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
+    kd<<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
   timing_end(family);
   MKS_CUDA(cudaGetLastError());
   return MKS_OK;
@@ -473,12 +505,16 @@ static int launch_shape(int family, const LinkT &fat, const LinkT &lng,
       return MKS_OK;
     }
   }
-  const bool pipe = sh.pipe != 0;
+  const bool pipe = sh.pipe != 0, persist = sh.persist != 0;
   switch (sh.NB) {
-  case 1: return launch_dslash_nb<R, LinkT, InT, OutT, 1, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block, pipe);
-  case 2: return launch_dslash_nb<R, LinkT, InT, OutT, 2, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block, pipe);
-  case 4: return launch_dslash_nb<R, LinkT, InT, OutT, 4, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block, pipe);
-  default: return launch_dslash_nb<R, LinkT, InT, OutT, 8, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block, pipe);
+  case 1:
+    return launch_dslash_nb<R, LinkT, InT, OutT, 1, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block, pipe, persist);
+  case 2:
+    return launch_dslash_nb<R, LinkT, InT, OutT, 2, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block, pipe, persist);
+  case 4:
+    return launch_dslash_nb<R, LinkT, InT, OutT, 4, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block, pipe, persist);
+  default:
+    return launch_dslash_nb<R, LinkT, InT, OutT, 8, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block, pipe, persist);
   }
 }
 
@@ -561,10 +597,10 @@ static int tune_shape(const LinkT &fat, const LinkT &lng, int nsrc, Shape *best)
     for (int G = 1; G <= 16; G *= 2) {
       const int NB = nbs[ib];
       if (G * NB < nsrc || G * NB > MAXSRC || (G * NB >= 2 * nsrc && G * NB > 1)) continue;
-      for (int cand = 0; cand < 4; cand++) {
-        const int block = (cand & 1) ? 256 : 128, pipe = cand >> 1;
+      for (int cand = 0; cand < 8; cand++) {
+        const int block = (cand & 1) ? 256 : 128, pipe = (cand >> 1) & 1, persist = cand >> 2;
         if (pipe && !pipe_enabled()) continue;
-        Shape sh = {G, NB, block, 0, pipe};
+        Shape sh = {G, NB, block, 0, pipe, persist};
         float tot = 0;
         for (int it = 0; it < 4; it++) {
           MKS_CUDA(cudaEventRecord(e0, c.stream));
@@ -634,9 +670,11 @@ static bool shape_override(int prec, int nsrc, bool epi, Shape *out) {
     if (sscanf(item.c_str(), "%d:%d:%d:%d:%d", &p, &n, &G, &NB, &B) == 5 && p == prec &&
         n == nsrc && G >= 1 && G <= 16 && (G & (G - 1)) == 0 && (NB == 1 || NB == 2 || NB == 4 || NB == 8) &&
         G * NB >= nsrc && G * NB <= MAXSRC && (B == 128 || B == 256)) {
-      // a trailing ":p" selects the software-pipelined kernel
-      const int pipe = item.size() > 2 && item.compare(item.size() - 2, 2, ":p") == 0;
-      *out = {G, NB, B, 0, pipe};
+      // trailing flags: ":p" the software-pipelined kernel, ":g" a persistent grid
+      const size_t f = item.find_first_not_of("0123456789:");
+      const std::string flags = f == std::string::npos ? "" : item.substr(f);
+      const int pipe = flags.find('p') != std::string::npos, persist = flags.find('g') != std::string::npos;
+      *out = {G, NB, B, 0, pipe, persist};
       return true;
     }
     int T, Rr;
@@ -1071,6 +1109,20 @@ static int true_residual(const LinkSlot &sl, int par, int nsrc, const double *ms
   return MKS_OK;
 }
 
+// Reliable-update batching factor f (MKS_RU_JOIN, default 1 = off): when a
+// source of a mixed-precision block asks for its FP64 reliable update (|r|
+// fell below delta * max|r|), every running source with |r| < f * delta *
+// max|r| takes its update in the same FP64 launch
+static double ru_join() {
+  static double v = -1;
+  if (v < 0) {
+    const char *e = getenv("MKS_RU_JOIN");
+    v = e ? atof(e) : 1.0;
+    if (!(v >= 1.0)) v = 1.0;
+  }
+  return v;
+}
+
 static int poll_interval() {
   static int v = -1;
   if (v < 0) {
@@ -1175,6 +1227,20 @@ static int block_cg_shifted(int slot, int par, int nsrc, const double *msq4, con
     for (int k = 0; k < nact; k++) {
       any_host |= hs[k].status == ST_HOST;
       any_run |= hs[k].status == ST_RUN;
+    }
+    if (any_host && mixed && !first && ru_join() > 1.0) {
+      // batch the FP64 reliable updates: a running source whose residual is
+      // within a factor ru_join() of its own trigger takes its update now,
+      // with the sources that asked, in one multi-source FP64 D
+      bool joined = false;
+      for (int k = 0; k < nact; k++) {
+        CgState &q = hs[k];
+        if (q.status == ST_RUN && sqrt(q.actual_rsq) < ru_join() * q.delta * q.maxrr) {
+          q.status = ST_HOST;
+          joined = true;
+        }
+      }
+      if (joined) MKS_TRY(write_states(S, nact, hs.data(), 1));
     }
     if (any_host) {
       // restart (FP64 CG) or reliable update (mixed): recompute the true residual
@@ -2534,5 +2600,5 @@ extern "C" int mks_tuned_variant(int prec, int nsrc, int epi) {
   if (prec < 0 || prec > 2 || nsrc < 1 || nsrc > MAXSRC) return MKS_ERR_ARG;
   const Shape &s = (epi ? g_shape_epi : g_shape)[prec][nsrc];
   if (s.G == 0) return MKS_ERR_STATE;
-  return s.tma ? 1 : (s.pipe ? 2 : 0);
+  return (s.tma ? 1 : (s.pipe ? 2 : 0)) + (s.persist ? 4 : 0);
 }
