@@ -234,12 +234,100 @@ def reference_arm(args):
 
 
 # ---------------------------------------------------------------- extras
+def family_times(lib, _lib):
+    fam = {}
+    for name, k in _lib.KERNEL_FAMILIES.items():
+        t, n = ctypes.c_double(), ctypes.c_longlong()
+        lib.mks_timing_get(k, ctypes.byref(t), ctypes.byref(n))
+        if n.value:
+            fam[name] = {"ms": t.value, "launches": n.value}
+    return fam
+
+
+def force_chain(m, lib, _lib, torch):
+    """The HISQ force workload on 16^3x32: a pseudofermion (Gaussian, even
+    sites), its 6-term rational function (residues in [0.1, 1], offsets
+    log-uniform in [1e-3, 1]) solved by the FP64 multi-shift to 1e-12, then
+    the fermion force of the 6 solutions (the force call moves the solutions
+    and momenta between host and device)."""
+    fdims = (16, 16, 16, 32)
+    m.set_lattice(fdims)
+    V = int(np.prod(fdims))
+    U = m.apply_phases(fdims, m.gen_thin_links(fdims, 77, LINK_A))
+    m.load_hisq_links(U)
+    rng = np.random.default_rng(4)
+    residues = list(np.sort(rng.uniform(0.1, 1.0, 6)))
+    offsets = np.logspace(-3, 0, 6)
+    phi = torch.from_numpy(m.gen_vector(fdims, 4444, m.EVEN)).cuda()
+    psim = [torch.zeros_like(phi) for _ in offsets]
+    VP = ctypes.c_void_p * 6
+    arg = _lib.InvertArg(2000, 5, m.EVEN, m.PREC_DOUBLE, 1e-12, 0.0, 0.1)
+    res = (_lib.InvertResult * 6)()
+    out = {}
+    for rep in range(2):
+        torch.cuda.synchronize()
+        t0 = time.time()
+        it = m.check(lib.mks_ks_multicg_offset_field_dev(phi.data_ptr(), VP(*[t.data_ptr() for t in psim]),
+                                                         offsets.ctypes.data_as(_lib.DP), 6, 0, ctypes.byref(arg),
+                                                         res), "force-chain multishift")
+        torch.cuda.synchronize()
+        t_solve = time.time() - t0
+        xxx = []
+        for t in psim:
+            y = t.cpu().numpy().copy()
+            y[V // 2:] = 0.0
+            d = np.zeros_like(y)
+            m.dslash_fn_field(y, d, m.ODD)
+            y[V // 2:] = d[V // 2:]   # X on even sites, D_oe X on odd sites
+            xxx.append(y)
+        mom = np.zeros((V, 4, 10))
+        t0 = time.time()
+        m.eo_fermion_force_multi(0.02, residues, xxx, mom)
+        t_force = time.time() - t0
+        out = {"multishift_fp64_1e-12_s": t_solve, "multishift_iters": it, "force_s": t_force,
+               "force_gflops_fp64": lib.mks_force_flops_last() / t_force / 1e9,
+               "force_includes": "host<->device copies of 6 vectors and the momenta"}
+    return out
+
+
+def rhmc_2p1p1(m, dims, steps=10, tau=1.0):
+    """The 2+1+1 HISQ RHMC trajectory (masses 0.0012 / 0.0363 / 0.432, the
+    rational functions of milc_qcd_gb300/data, leapfrog, seeded exp(i 0.2 H)
+    links), once with FP32 solves and force arithmetic and once all FP64
+    from the same start: time per trajectory and Delta H of both."""
+    from milc_qcd_gb300.rhmc import load_rhmc_params, update
+    w = dict(RHMC_WORKLOAD)
+    pfs = load_rhmc_params(os.path.join(ROOT, "milc_qcd_gb300", "data", w["rationals"]))
+    n = len(pfs)
+    m.set_lattice(dims)
+    V = int(np.prod(dims))
+    U0 = m.gen_thin_links(dims, w["seed"], 0.2)
+    runs = {}
+    for name, prec in (("f32", m.PREC_SINGLE), ("f64", m.PREC_DOUBLE)):
+        m.gauge_load(U0)
+        m.mom_load(np.zeros((V, 4, 10)))
+        m.rng_seed(w["seed"])
+        r = update(pfs, w["beta"], w["u0"], w["nflavors"], tau / steps, steps, "leapfrog",
+                   [w["resid_md"]] * n, [w["resid_fa"]] * n, [w["resid_gr"]] * n, w["max_cg"], prec, prec, prec,
+                   5, True, prec_force=prec)
+        runs[name] = {k: r[k] for k in ("t_total", "t_solve", "t_fermion_force", "t_gauge_force", "t_links",
+                                         "cg_iters", "n_solves", "unconverged", "delta_s")}
+    return {"lattice": list(dims), "masses": [0.0012, 0.0363, 0.432], "pseudofermions": n, "steps": steps,
+            "tau": tau, "integrator": "leapfrog", "poles": [p.MD.order for p in pfs], "runs": runs,
+            "s_per_trajectory_f32": runs["f32"]["t_total"], "s_per_trajectory_f64": runs["f64"]["t_total"],
+            "delta_h_f32_minus_f64": runs["f32"]["delta_s"] - runs["f64"]["delta_s"]}
+
+
 def extras(m, lib, _lib, torch, srcs):
     """Figures for the other workloads of the same family, measured after the
     headline (not part of `value`): the multi-source sweep N = 1, 4, 8, 16
-    (32^3x64, FP32 inner solve), the 11-offset multi-shift solve (32^3x64,
+    (32^3x64, FP32 inner solve); the 11-offset multi-shift solve (32^3x64,
     sigma_i = 4m^2 + s_i, s_i log-uniform in [1e-4, 1]) in FP64 and mixed
-    precision, and the HISQ fermion force on 16^3x32 (6 terms)."""
+    precision, with the rooflines of its update kernel and its D_eo pair; the
+    HISQ force chain on 16^3x32 (6-term multi-shift to 1e-12, then the force);
+    MILC's 2+1 RHMC regression set-up on 16^3x32; and the 2+1+1 RHMC
+    trajectory on 48^3x96 in FP32 and FP64 from the same start (Delta H of
+    both; MKS_BENCH_NO_48=1 leaves it out)."""
     out = {}
     sweep = {}
     for n in (1, 4, 8, 16):
@@ -266,10 +354,15 @@ def extras(m, lib, _lib, torch, srcs):
     d_p = [torch.zeros_like(d_b) for _ in sig]
     VP = ctypes.c_void_p * len(sig)
     ms = {}
+    Vh = int(np.prod(DIMS)) // 2
+    peak, _ = peaks()
     for name, prec in (("f64", m.PREC_DOUBLE), ("single", m.PREC_SINGLE), ("half", m.PREC_HALF)):
         arg = _lib.InvertArg(1000, 10, m.EVEN, prec, RESID, 0.0, 0.1)
         res = (_lib.InvertResult * len(sig))()
         for rep in range(2):
+            if rep == 1:
+                lib.mks_timing_reset()
+                lib.mks_timing_enable(1)
             torch.cuda.synchronize()
             t0 = time.time()
             it = m.check(lib.mks_ks_multicg_offset_field_dev(d_b.data_ptr(), VP(*[t.data_ptr() for t in d_p]),
@@ -277,23 +370,39 @@ def extras(m, lib, _lib, torch, srcs):
                                                              ctypes.byref(arg), res), "multishift")
             torch.cuda.synchronize()
             dt = time.time() - t0
+        lib.mks_timing_enable(0)
+        fam = family_times(lib, _lib)
         ms[name] = {"s": dt, "iters": it, "max_final_rsq": max(res[k].final_rsq for k in range(len(sig))),
-                    "converged": all(res[k].converged for k in range(len(sig)))}
+                    "converged": all(res[k].converged for k in range(len(sig))), "kernel_ms": fam}
+        # rooflines of the multi-shift iteration's two kernels: the update
+        # kernel (OpShiftUpdate) and the single-source D_eo pair
+        n_it, n_upd = ctypes.c_longlong(), ctypes.c_longlong()
+        lib.mks_multishift_counts(ctypes.byref(n_it), ctypes.byref(n_upd))
+        vb = {m.PREC_DOUBLE: 48, m.PREC_SINGLE: 24, m.PREC_HALF: 24}[prec]  # update-kernel vectors
+        if "shift" in fam and fam["shift"]["launches"]:
+            upd_bytes = (4 * n_it.value + 4 * n_upd.value) * vb * Vh
+            gbs = upd_bytes / (fam["shift"]["ms"] * 1e-3) / 1e9
+            ms[name]["roofline_shift_update"] = {
+                "bytes": upd_bytes, "ms": fam["shift"]["ms"], "gbs": gbs, "frac": gbs / peak,
+                "per_site": "(4 + 4 x shifts advanced) vectors of %d B per iteration; %d iterations, %d shift "
+                            "updates" % (vb, n_it.value, n_upd.value)}
+        dfam = {m.PREC_DOUBLE: "dslash_f64", m.PREC_SINGLE: "dslash_f32", m.PREC_HALF: "dslash_f16"}[prec]
+        if prec != m.PREC_DOUBLE and dfam in fam and fam[dfam]["launches"]:
+            # D pair per iteration: links twice (16 x 72 B FP32, 16 x 36 B FP16), input and output
+            # vectors, and p and r of the fused epilogue (FP32); the reliable updates' FP64 D is
+            # timed apart
+            lk = 1152 if prec == m.PREC_SINGLE else 576
+            vin = 24 if prec == m.PREC_SINGLE else 16
+            pair = (2 * lk + (vin + vin) + (vin + 24 + 48)) * Vh
+            d_ms = fam[dfam]["ms"] / (fam[dfam]["launches"] / 2)
+            gbs = pair / (d_ms * 1e-3) / 1e9
+            ms[name]["roofline_dslash_pair"] = {"bytes_per_pair": pair, "ms_per_pair": d_ms, "gbs": gbs,
+                                                "frac": gbs / peak}
     out["multishift_11_offsets"] = ms
-    fdims = (16, 16, 16, 32)
-    m.set_lattice(fdims)
-    U = m.apply_phases(fdims, m.gen_thin_links(fdims, 77, LINK_A))
-    m.load_hisq_links(U)
-    xxx = [m.gen_vector(fdims, 300 + j, m.EVENANDODD) for j in range(6)]
-    res6 = list(np.linspace(0.1, 1.0, 6))
-    mom = np.zeros((int(np.prod(fdims)), 4, 10))
-    m.eo_fermion_force_multi(0.01, res6, xxx, mom)
-    t0 = time.time()
-    m.eo_fermion_force_multi(0.01, res6, xxx, mom)
-    dt = time.time() - t0
-    out["hisq_force_16c32_6terms"] = {"s_per_call": dt, "gflops_fp64": lib.mks_force_flops_last() / dt / 1e9,
-                                      "includes": "host<->device copies of 6 vectors and the momenta"}
+    out["force_chain_16c32_6terms"] = force_chain(m, lib, _lib, torch)
     out["rhmc_trajectory"] = rhmc_trajectory(m, RHMC_DIMS)
+    if not os.environ.get("MKS_BENCH_NO_48"):
+        out["rhmc_2p1p1_48c96"] = rhmc_2p1p1(m, (48, 48, 48, 96))
     m.set_lattice(DIMS)
     return out
 
