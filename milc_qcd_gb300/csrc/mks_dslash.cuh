@@ -194,8 +194,11 @@ __device__ __forceinline__ void site_terms(const LinkT &fat, const LinkT &lng, c
 // live = false (a TMA tile whose staged links did not arrive): the thread
 // computes and writes nothing but still takes part in the grid reduction
 // with zero sums, so the arrival counters return to zero as in every launch
+// LOOP = true: the CTA loops over site blocks (persistent grid, a.nvb);
+// a separate instantiation, since the loop costs registers (loop-invariant
+// values held across it)
 template <typename R, class LinkT, class InT, class OutT, int NB, int EPI, int NSUM, class Fin, bool TMA = false,
-          bool PIPE = false>
+          bool PIPE = false, bool LOOP = false>
 __device__ __forceinline__ void dslash_body(const LinkT &fat, const LinkT &lng,
                                             const DslashArgs<InT, OutT, typename EpiLoad<R>::type> &a,
                                             const Fin &fin, const TileSmem ts = TileSmem{nullptr, 0},
@@ -218,8 +221,8 @@ __device__ __forceinline__ void dslash_body(const LinkT &fat, const LinkT &lng,
   // site blocks: one per CTA, or (a.nvb > gridDim.x) a persistent grid that
   // loops over them in the same order, so each CTA reduces its dot products
   // once at the end
-  const int nvb = (!TMA && a.nvb > 0) ? a.nvb : (int)gridDim.x;
-  for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+  const int nvb = (LOOP && a.nvb > 0) ? a.nvb : (int)gridDim.x;
+  auto site_block = [&](const int vb) {
   // a plain D may sweep the sites from the end: it then reads first the part
   // of its input that the previous kernel wrote last (still in L2) and
   // leaves the start of its output in L2 for a following forward sweep
@@ -339,7 +342,13 @@ __device__ __forceinline__ void dslash_body(const LinkT &fat, const LinkT &lng,
       else a.out[S].store(h, Vh, acc[s]);
     }
   }
-  }  // site blocks
+  };  // site_block
+  if constexpr (LOOP) {
+#pragma unroll 1
+    for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) site_block(vb);
+  } else {
+    site_block((int)blockIdx.x);
+  }
   if (NSUM > 0) {
     __shared__ double smem[(256 / 32 + 1) * MAXSRC * 3];
     __shared__ double tot[MAXSRC * 3];
@@ -363,6 +372,17 @@ __global__ void __launch_bounds__(256)
 k_dslash(const LinkT fat, const LinkT lng, const DslashArgs<InT, OutT, typename EpiLoad<R>::type> a,
          const Fin fin) {
   dslash_body<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin>(fat, lng, a, fin);
+}
+
+// the multi-source shapes on a persistent grid: as many CTAs as fit on the
+// GPU loop over the site blocks (a.nvb), so a fused-epilogue launch reduces
+// its dot products once per CTA; at least 3 resident 256-thread blocks per
+// SM are asked of the register allocator (the loop holds more values live)
+template <typename R, class LinkT, class InT, class OutT, int NB, int EPI, int NSUM, class Fin>
+__global__ void __launch_bounds__(256, 3)
+k_dslash_g(const LinkT fat, const LinkT lng, const DslashArgs<InT, OutT, typename EpiLoad<R>::type> a,
+           const Fin fin) {
+  dslash_body<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin, false, false, true>(fat, lng, a, fin);
 }
 
 // the same shapes with the link loads software-pipelined one term deep

@@ -449,23 +449,24 @@ static int launch_dslash_nb(int family, const LinkT &fat, const LinkT &lng,
   auto kp = k_dslash_p<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin>;
   auto k1 = k_dslash1<R, LinkT, InT, OutT, EPI, NSUM, Fin>;
   auto kd = k_dslash<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin>;
-  const bool one = !pipe && NB == 1 && a.groups == 1 && block == 256;
+  auto kg = k_dslash_g<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin>;
+  if (persist) pipe = false;  // the persistent kernel loads directly
+  const bool one = !pipe && !persist && NB == 1 && a.groups == 1 && block == 256;
   int grid = nvb;
   a.nvb = 0;
   if (persist) {
-    const int nres = pipe ? resident_blocks(kp, block) : (one ? resident_blocks(k1, block) : resident_blocks(kd, block));
-    const int cap = nres * c.sm_count;
-    if (cap < nvb) {
-      grid = cap;
-      a.nvb = nvb;
-    }
+    const int cap = resident_blocks(kg, block) * c.sm_count;
+    if (cap < nvb) grid = cap;
+    a.nvb = nvb;
   }
   if (NSUM > 0) {
     MKS_TRY(ensure_red(NSUM * a.groups * NB, grid));
     a.red = c.red;
   }
   timing_begin(family);
-  if (pipe)
+  if (persist)
+    kg<<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
+  else if (pipe)
     kp<<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
   else if (one)
     k1<<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
@@ -599,7 +600,7 @@ static int tune_shape(const LinkT &fat, const LinkT &lng, int nsrc, Shape *best)
       if (G * NB < nsrc || G * NB > MAXSRC || (G * NB >= 2 * nsrc && G * NB > 1)) continue;
       for (int cand = 0; cand < 8; cand++) {
         const int block = (cand & 1) ? 256 : 128, pipe = (cand >> 1) & 1, persist = cand >> 2;
-        if (pipe && !pipe_enabled()) continue;
+        if ((pipe && !pipe_enabled()) || (pipe && persist)) continue;
         Shape sh = {G, NB, block, 0, pipe, persist};
         float tot = 0;
         for (int it = 0; it < 4; it++) {
