@@ -185,7 +185,7 @@ def cpu_extras(threads=None):
 # D_eo family (mean of the plain D and the fused CG-epilogue launch), from
 # ncu captures of this benchmark on GB300 (summaries under profiles/)
 MEASURED_TRAFFIC = {
-    ("single", 8, (32, 32, 32, 64)): 0.5 * (1.614e9 + 2.095e9),
+    ("single", 8, (32, 32, 32, 64), True): 0.5 * (1.614e9 + 2.095e9),
 }
 
 # FP64 CG iterations to |r|/|b| = 1e-10 on this workload (32^3x64, m = 0.01,
@@ -549,17 +549,28 @@ def gpu_arm(args):
                                ctypes.byref(tma)) == 0:
         shapes["D+epilogue"] = {"G": G.value, "NB": nb.value, "block": blk.value, "tma": tma.value,
                                 "kernel": variant(lib.mks_tuned_variant(prec, N, 1))}
-    dslash_ms = tot_ms.value / max(nl.value, 1)
+    # Launches that did work: a batch of iterations replayed as a graph stops
+    # early (its remaining kernels return at once) when a source asks for a
+    # reliable update, so the launch count includes such empty launches.  The
+    # block runs as many CG iterations as its slowest source, two D_eo each
+    # (final_iters counts the CG iterations, the initial true residual and
+    # the reliable updates).
+    cg_iters = max(res[k].final_iters - 1 - res[k].reliable_updates for k in range(N))
+    d_executed = 2 * cg_iters * args.steps if N > 1 and prec != m.PREC_DOUBLE else nl.value
+    dslash_ms = tot_ms.value / max(d_executed, 1)
     Vh = V // 2
+    # the second D of an iteration carries the fused CG epilogue unless the
+    # epilogue runs as its own kernel (then no fused-epilogue shape was tuned)
+    fused = lib.mks_tuned_shape_epi(prec, N, None, None, None, None) == 0
     if prec == m.PREC_HALF:
         # K1: half links + half in/out (+norms); K2: half links + half in, f32 out, f32 p and r read
         per_site = 16 * 18 * 2 + N * 0.5 * ((16 + 16) + (16 + 24 + 24 + 24))
     elif prec == m.PREC_SINGLE:
-        per_site = 16 * 18 * 4 + N * 0.5 * ((24 + 24) + (24 + 24 + 24 + 24))
+        per_site = 16 * 18 * 4 + N * (0.5 * ((24 + 24) + (24 + 24 + 24 + 24)) if fused else (24 + 24))
     else:
         per_site = 16 * 18 * 8 + N * 0.5 * ((48 + 48) + (48 + 48 + 48 + 48))
     alg_bytes = per_site * Vh
-    traffic = MEASURED_TRAFFIC.get((args.prec, N, tuple(DIMS)))
+    traffic = MEASURED_TRAFFIC.get((args.prec, N, tuple(DIMS), fused))
     peak, peak_kind = peaks()
     achieved = alg_bytes / (dslash_ms * 1e-3) / 1e9
     # plain FP64 D_eo and FP32 D_eo standalone timings (L2 flushed between launches)
@@ -604,9 +615,10 @@ def gpu_arm(args):
         "dslash_gbs": {"f32_single_rhs": gbs32, "f32_ms": ms32.value, "f64_ms": ms64.value,
                        "f64_gflops": 1146.0 * Vh / (ms64.value * 1e-3) / 1e9},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "traffic_unit": "bytes per launch (mean of the D and D+epilogue launches)",
-                     "kernel": "k_dslash (%s, nsrc=%d)" % (args.prec, N),
-                     "peak_source": peak_kind, "avg_launch_ms": dslash_ms, "launches": nl.value},
+                     "traffic": traffic, "traffic_unit": "bytes per launch (ncu DRAM read + write)",
+                     "kernel": "k_dslash (%s, nsrc=%d%s)" % (args.prec, N, "" if fused else ", plain D pair"),
+                     "peak_source": peak_kind, "avg_launch_ms": dslash_ms, "algorithmic_bytes_per_launch": alg_bytes,
+                     "launches_executed": d_executed, "launches_issued": nl.value},
         # the C ABI moves the solved parity's half of each field: source and
         # initial guess in, solution out
         "e2e": {"value": e2e_per_src, "unit": "s/solve", "h2d_bytes_per_step": N * bytes_field,

@@ -90,7 +90,8 @@ typedef struct {
 int mks_init(int device);
 int mks_finalize(void);
 const char *mks_error_string(int status);
-/* Lattice extents (all even).  Frees every cached field of another size. */
+/* Lattice extents (all even and at least 4: the Naik term reaches 3 sites).
+ * Frees every cached field of another size. */
 int mks_set_lattice(const int dims[4]);
 
 /* ------------------------------------------------------------------ */

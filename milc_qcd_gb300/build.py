@@ -21,6 +21,9 @@ NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-fopenmp", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
+# extra nvcc flags for measurement builds (e.g. "-DMKS_NBR_LEX=0"); objects
+# are rebuilt when the flags change
+EXTRA_NVFLAGS = os.environ.get("MKS_NVFLAGS", "").split()
 CFLAGS = ["-O2", "-g", "-std=gnu99", "-fPIC", "-fopenmp", "-Wall", "-Wno-unused-function",
           "-I" + os.path.join(ROOT, "include")]
 
@@ -49,12 +52,18 @@ def build(verbose=False, extra_nvflags=()):
     """Compile the library if needed and return its path."""
     os.makedirs(OBJDIR, exist_ok=True)
     deps = _headers()
+    flags = NVFLAGS + EXTRA_NVFLAGS + list(extra_nvflags)
+    stamp = os.path.join(OBJDIR, "nvflags")
+    old = open(stamp).read() if os.path.exists(stamp) else None
+    if old != " ".join(flags):
+        with open(stamp, "w") as f:
+            f.write(" ".join(flags))
     jobs, objs = [], []
     for src in sorted(glob.glob(os.path.join(CSRC, "*.cu"))):
         obj = os.path.join(OBJDIR, os.path.basename(src) + ".o")
         objs.append(obj)
-        if _stale(obj, src, deps):
-            jobs.append(([NVCC] + ARCH + NVFLAGS + list(extra_nvflags) + ["-c", src, "-o", obj], obj))
+        if _stale(obj, src, deps + [stamp]):
+            jobs.append(([NVCC] + ARCH + flags + ["-c", src, "-o", obj], obj))
     for src in sorted(glob.glob(os.path.join(CSRC, "*.c"))):
         obj = os.path.join(OBJDIR, os.path.basename(src) + ".o")
         objs.append(obj)

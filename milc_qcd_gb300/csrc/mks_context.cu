@@ -437,8 +437,10 @@ int mks_finalize(void) {
 int mks_set_lattice(const int dims[4]) {
   MKS_TRY(check_ready(false));
   if (!dims) return MKS_ERR_ARG;
+  // even extents of at least 4: the Naik term reaches 3 sites, and a hop of
+  // 3 must wrap at most once
   for (int d = 0; d < 4; d++)
-    if (dims[d] < 2 || (dims[d] & 1)) return MKS_ERR_ARG;
+    if (dims[d] < 4 || (dims[d] & 1)) return MKS_ERR_ARG;
   Context &c = g_ctx;
   size_t V = (size_t)dims[0] * dims[1] * dims[2] * dims[3];
   if (V / 2 > (size_t)0x3fffffff) return MKS_ERR_ARG;  // checkerboard index is 32-bit

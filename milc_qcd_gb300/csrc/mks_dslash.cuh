@@ -72,19 +72,36 @@ struct NoFinish {
 #define MKS_DSLASH1_MINB 4
 #endif
 
-// checkerboard indices of the +-1 and +-3 neighbours along mu of the site with coordinates c0
+// checkerboard indices of the +-1 and +-3 neighbours along mu of the site with
+// coordinates c0: from the site's lexicographic index, one add, one select
+// and one shift each (a hop of k along mu moves the lexicographic index by
+// k * stride, less extent * stride where it wraps; extents are >= 4, so a
+// hop of 3 wraps at most once)
+#ifndef MKS_NBR_LEX
+#define MKS_NBR_LEX 1
+#endif
 __device__ __forceinline__ void nbr4(const Geom &g, const int c0[4], const int L[4], int mu, int &hf1, int &hb1,
                                      int &hf3, int &hb3) {
-  int cf1[4] = {c0[0], c0[1], c0[2], c0[3]}, cb1[4] = {c0[0], c0[1], c0[2], c0[3]};
-  int cf3[4] = {c0[0], c0[1], c0[2], c0[3]}, cb3[4] = {c0[0], c0[1], c0[2], c0[3]};
-  cf1[mu] = wrap_add(c0[mu], 1, L[mu]);
-  cb1[mu] = wrap_add(c0[mu], -1, L[mu]);
-  cf3[mu] = wrap_add(c0[mu], 3, L[mu]);
-  cb3[mu] = wrap_add(c0[mu], -3, L[mu]);
-  hf1 = cb_index(g, cf1[0], cf1[1], cf1[2], cf1[3]);
-  hb1 = cb_index(g, cb1[0], cb1[1], cb1[2], cb1[3]);
-  hf3 = cb_index(g, cf3[0], cf3[1], cf3[2], cf3[3]);
-  hb3 = cb_index(g, cb3[0], cb3[1], cb3[2], cb3[3]);
+  if (!MKS_NBR_LEX) {  // the same indices from the shifted coordinates
+    int cf1[4] = {c0[0], c0[1], c0[2], c0[3]}, cb1[4] = {c0[0], c0[1], c0[2], c0[3]};
+    int cf3[4] = {c0[0], c0[1], c0[2], c0[3]}, cb3[4] = {c0[0], c0[1], c0[2], c0[3]};
+    cf1[mu] = wrap_add(c0[mu], 1, L[mu]);
+    cb1[mu] = wrap_add(c0[mu], -1, L[mu]);
+    cf3[mu] = wrap_add(c0[mu], 3, L[mu]);
+    cb3[mu] = wrap_add(c0[mu], -3, L[mu]);
+    hf1 = cb_index(g, cf1[0], cf1[1], cf1[2], cf1[3]);
+    hb1 = cb_index(g, cb1[0], cb1[1], cb1[2], cb1[3]);
+    hf3 = cb_index(g, cf3[0], cf3[1], cf3[2], cf3[3]);
+    hb3 = cb_index(g, cb3[0], cb3[1], cb3[2], cb3[3]);
+    return;
+  }
+  const int i = c0[0] + g.nx * (c0[1] + g.ny * (c0[2] + g.nz * c0[3]));
+  const int S = mu == 0 ? g.sx : (mu == 1 ? g.sy : (mu == 2 ? g.sz : g.st));
+  const int LS = L[mu] * S, c = c0[mu];
+  hf1 = (i + S - (c + 1 >= L[mu] ? LS : 0)) >> 1;
+  hb1 = (i - S + (c < 1 ? LS : 0)) >> 1;
+  hf3 = (i + 3 * S - (c + 3 >= L[mu] ? LS : 0)) >> 1;
+  hb3 = (i - 3 * S + (c < 3 ? LS : 0)) >> 1;
 }
 
 // ---- links of a tile staged in shared memory by the TMA engine ----
@@ -366,9 +383,15 @@ __device__ __forceinline__ void dslash_body(const LinkT &fat, const LinkT &lng,
   }
 }
 
-// the multi-source shapes (G threads per site x NB sources per thread)
+// the multi-source shapes (G threads per site x NB sources per thread);
+// the FP32/FP16 plain D with up to 4 sources per thread is held to 64
+// registers (4 resident 256-thread blocks per SM), which it needs without
+// spilling
+#ifndef MKS_DSLASH_MINB
+#define MKS_DSLASH_MINB 4
+#endif
 template <typename R, class LinkT, class InT, class OutT, int NB, int EPI, int NSUM, class Fin>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, (sizeof(R) == 4 && NB <= 4 && EPI == EPI_PLAIN && !LinkT::scaled) ? MKS_DSLASH_MINB : 0)
 k_dslash(const LinkT fat, const LinkT lng, const DslashArgs<InT, OutT, typename EpiLoad<R>::type> a,
          const Fin fin) {
   dslash_body<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin>(fat, lng, a, fin);
