@@ -208,18 +208,113 @@ __device__ __forceinline__ void site_terms(const LinkT &fat, const LinkT &lng, c
   }
 }
 
+// ---- cp.async helpers (per-thread asynchronous global -> shared copies) ----
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+               "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+               "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// The 16 terms of one output site with the FP32 links fetched ahead into
+// shared memory by cp.async (a ring of STAGES link buffers per site): the
+// copies of the next STAGES-1 terms' links are in flight while this term's
+// mat-vecs run, and an in-flight copy holds no register.  The G threads of a
+// site share its buffers (each copies some of the link's five 16/8-byte
+// pieces) and sit in one warp; __syncwarp orders a buffer's copies before
+// its reads and its reads before it is refilled.  Every thread of the warp
+// runs the loop; `valid` marks the threads that own a site.  Buffer layout
+// per stage: four float4 planes and one float2 plane of the block's sites.
+template <int STAGES>
+__device__ __forceinline__ void async_issue(const LinkF32 &fat, const LinkF32 &lng, int term, int par, int opar,
+                                            int h, int hb1, int hb3, int Vh, int grp, int G, unsigned char *buf,
+                                            int spb, int j) {
+  const int mu = term >> 2, kind = term & 3;
+  const LinkF32 &L = (kind & 1) ? lng : fat;
+  const int sp = kind < 2 ? par : opar;
+  const int idx = kind < 2 ? h : (kind == 2 ? hb1 : hb3);
+  for (int k = grp; k < 5; k += G) {
+    if (k < 4)
+      cp_async16(buf + (size_t)k * 16 * spb + 16 * j, L.a + ((size_t)(sp * 4 + mu) * 4 + k) * Vh + idx);
+    else
+      cp_async8(buf + (size_t)64 * spb + 8 * j, L.b + (size_t)(sp * 4 + mu) * Vh + idx);
+  }
+}
+
+template <class InT, int NB, int STAGES>
+__device__ __forceinline__ void site_terms_async(const LinkF32 &fat, const LinkF32 &lng, const InT *in, int nsrc,
+                                                 int grp, int G, const Geom &g, int par, int h, const int c0[4],
+                                                 V3<float> (&acc)[NB], bool valid, unsigned char *smem) {
+  const int Vh = g.Vh, opar = 1 - par;
+  const int L[4] = {g.nx, g.ny, g.nz, g.nt};
+  const int spb = (int)blockDim.x / G, j = (int)threadIdx.x / G;
+  const size_t stage_bytes = (size_t)72 * spb;
+  // neighbour indices per direction, for the vectors and the backward links
+  int nb[4][4];
+#pragma unroll
+  for (int mu = 0; mu < 4; mu++) nbr4(g, c0, L, mu, nb[mu][0], nb[mu][1], nb[mu][2], nb[mu][3]);
+#pragma unroll
+  for (int t = 0; t < STAGES - 1; t++) {
+    if (valid)
+      async_issue<STAGES>(fat, lng, t, par, opar, h, nb[t >> 2][1], nb[t >> 2][3], Vh, grp, G,
+                          smem + (size_t)t * stage_bytes, spb, j);
+    cp_async_commit();
+  }
+#pragma unroll
+  for (int term = 0; term < 16; term++) {
+    const int nt = term + STAGES - 1;
+    __syncwarp();  // every lane has read the buffer about to be refilled
+    if (nt < 16 && valid)
+      async_issue<STAGES>(fat, lng, nt, par, opar, h, nb[nt >> 2][1], nb[nt >> 2][3], Vh, grp, G,
+                          smem + (size_t)(nt % STAGES) * stage_bytes, spb, j);
+    cp_async_commit();
+    cp_async_wait<STAGES - 1>();  // this thread's pieces of `term` have landed
+    __syncwarp();                 // and the other threads' of the site
+    if (!valid) continue;
+    const unsigned char *b = smem + (size_t)(term % STAGES) * stage_bytes;
+    M3<float> U;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const float4 q = *reinterpret_cast<const float4 *>(b + (size_t)k * 16 * spb + 16 * j);
+      U.e[(2 * k) / 3][(2 * k) % 3] = {q.x, q.y};
+      U.e[(2 * k + 1) / 3][(2 * k + 1) % 3] = {q.z, q.w};
+    }
+    const float2 e8 = *reinterpret_cast<const float2 *>(b + (size_t)64 * spb + 8 * j);
+    U.e[2][2] = {e8.x, e8.y};
+    const int mu = term >> 2, kind = term & 3;
+    const int n = nb[mu][kind == 0 ? 0 : (kind == 1 ? 2 : (kind == 2 ? 1 : 3))];
+#pragma unroll
+    for (int s = 0; s < NB; s++) {
+      if (grp * NB + s >= nsrc) continue;
+      const V3<float> v = in[grp * NB + s].load(n, Vh);
+      if (kind < 2) mv_acc(U, v, acc[s]);
+      else amv_sub(U, v, acc[s]);
+    }
+  }
+}
+
 // live = false (a TMA tile whose staged links did not arrive): the thread
 // computes and writes nothing but still takes part in the grid reduction
 // with zero sums, so the arrival counters return to zero as in every launch
 // LOOP = true: the CTA loops over site blocks (persistent grid, a.nvb);
 // a separate instantiation, since the loop costs registers (loop-invariant
 // values held across it)
+// ASYNC = STAGES > 0: FP32 links fetched ahead by cp.async into the dynamic
+// shared memory `asm_base` (site_terms_async)
 template <typename R, class LinkT, class InT, class OutT, int NB, int EPI, int NSUM, class Fin, bool TMA = false,
-          bool PIPE = false, bool LOOP = false>
+          bool PIPE = false, bool LOOP = false, int ASYNC = 0>
 __device__ __forceinline__ void dslash_body(const LinkT &fat, const LinkT &lng,
                                             const DslashArgs<InT, OutT, typename EpiLoad<R>::type> &a,
                                             const Fin &fin, const TileSmem ts = TileSmem{nullptr, 0},
-                                            const bool live = true) {
+                                            const bool live = true, unsigned char *asm_base = nullptr) {
   typedef typename EpiLoad<R>::type EpiT;
   if (a.skip && *a.skip) return;
   const Geom &g = a.g;
@@ -261,16 +356,19 @@ __device__ __forceinline__ void dslash_body(const LinkT &fat, const LinkT &lng,
       }
     }
   }
-  if (h < Vh && live) {
-    int x, y, z, t;
-    site_coords(g, par, h, x, y, z, t);
+  const bool valid = h < Vh && live;
+  if (valid || ASYNC > 0) {  // the async loop runs on every lane of the warp
+    int x = 0, y = 0, z = 0, t = 0;
+    if (valid) site_coords(g, par, h, x, y, z, t);
     V3<R> acc[NB];
 #pragma unroll
     for (int s = 0; s < NB; s++)
 #pragma unroll
       for (int c = 0; c < 3; c++) acc[s].c[c] = {R(0), R(0)};
     const int c0[4] = {x, y, z, t};
-    if constexpr (!TMA) {
+    if constexpr (ASYNC > 0) {
+      site_terms_async<InT, NB, ASYNC>(fat, lng, a.in, a.nsrc, grp, G, g, par, h, c0, acc, valid, asm_base);
+    } else if constexpr (!TMA) {
       site_terms<R, LinkT, InT, NB, PIPE>(fat, lng, a.in, a.nsrc, grp, g, par, h, c0, acc);
     } else {
     const int L[4] = {g.nx, g.ny, g.nz, g.nt};
@@ -327,7 +425,7 @@ __device__ __forceinline__ void dslash_body(const LinkT &fat, const LinkT &lng,
 #pragma unroll
     for (int s = 0; s < NB; s++) {
       const int S = grp * NB + s;
-      if (S >= a.nsrc) continue;
+      if (S >= a.nsrc || !valid) continue;
       if (EPI == EPI_AXPY) {
         const V3<R> p = a.p[S].load(h, Vh);
         const R cf = (R)a.coef[S];
@@ -406,6 +504,19 @@ __global__ void __launch_bounds__(256, 3)
 k_dslash_g(const LinkT fat, const LinkT lng, const DslashArgs<InT, OutT, typename EpiLoad<R>::type> a,
            const Fin fin) {
   dslash_body<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin, false, false, true>(fat, lng, a, fin);
+}
+
+// the multi-source FP32 shapes with the links fetched ahead into shared
+// memory by cp.async, STAGES link buffers per site (dynamic shared memory
+// STAGES x 72 B x sites per block); at least 3 resident 256-thread blocks
+// per SM (80 registers: 4 sources per thread spill a few bytes, a bound of 4
+// blocks spills hundreds)
+template <class InT, class OutT, int NB, int EPI, int NSUM, class Fin, int STAGES>
+__global__ void __launch_bounds__(256, 3)
+k_dslash_a(const LinkF32 fat, const LinkF32 lng, const DslashArgs<InT, OutT, VecF32> a, const Fin fin) {
+  extern __shared__ __align__(16) unsigned char adsm[];
+  dslash_body<float, LinkF32, InT, OutT, NB, EPI, NSUM, Fin, false, false, false, STAGES>(
+      fat, lng, a, fin, TileSmem{nullptr, 0}, true, adsm);
 }
 
 // the same shapes with the link loads software-pipelined one term deep

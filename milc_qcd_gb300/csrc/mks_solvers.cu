@@ -394,7 +394,9 @@ static LinkSet16 links16(const LinkSlot &s) {
 // persist = 1: a persistent grid (as many CTAs as fit on the GPU at once)
 // that loops over the site blocks, so a fused-epilogue launch reduces its
 // dot products once per CTA rather than once per site block
-struct Shape { int G, NB, block, tma, pipe, persist; };
+// as = 2 or 3: FP32 links fetched ahead into shared memory by cp.async with
+// that many link buffers per site (k_dslash_a)
+struct Shape { int G, NB, block, tma, pipe, persist, as; };
 static Shape g_shape[3][MAXSRC + 1];      // [prec][nsrc], G == 0: not chosen yet
 static Shape g_shape_epi[3][MAXSRC + 1];  // the same for the fused-epilogue launches
 static void shapes_reset() {
@@ -413,7 +415,7 @@ void tma_disable() {
   for (auto *tab : {g_shape, g_shape_epi})
     for (int p = 0; p < 3; p++)
       for (int n = 0; n <= MAXSRC; n++)
-        if (tab[p][n].tma) tab[p][n] = Shape{0, 0, 0, 0, 0, 0};
+        if (tab[p][n].tma) tab[p][n] = Shape{0, 0, 0, 0, 0, 0, 0};
   graphs_free_all();
 }
 // true once after tma_disable: the failed call may be repeated
@@ -473,10 +475,32 @@ template <class K> static int resident_blocks(K kernel, int block) {
 template <typename R, class LinkT, class InT, class OutT, int NB, int EPI, int NSUM, class Fin>
 static int launch_dslash_nb(int family, const LinkT &fat, const LinkT &lng,
                             DslashArgs<InT, OutT, typename EpiLoad<R>::type> &a, const Fin &fin, int block,
-                            bool pipe, bool persist) {
+                            bool pipe, bool persist, int as = 0) {
   Context &c = ctx();
   size_t threads = (size_t)c.Vh * a.groups;
   const int nvb = (int)((threads + block - 1) / block);
+  if constexpr (std::is_same<LinkT, LinkF32>::value) {
+    if (as == 2 || as == 3) {
+      const int grid = nvb;
+      a.nvb = 0;
+      const size_t smem = (size_t)as * 72 * (block / a.groups);
+      if (NSUM > 0) {
+        MKS_TRY(ensure_red(NSUM * a.groups * NB, grid));
+        a.red = c.red;
+      }
+      auto ka = as == 2 ? k_dslash_a<InT, OutT, NB, EPI, NSUM, Fin, 2> : k_dslash_a<InT, OutT, NB, EPI, NSUM, Fin, 3>;
+      static bool attr[2] = {false, false};
+      if (smem > 48 * 1024 && !attr[as - 2]) {
+        MKS_CUDA(cudaFuncSetAttribute(ka, cudaFuncAttributeMaxDynamicSharedMemorySize, 3 * 72 * 256));
+        attr[as - 2] = true;
+      }
+      timing_begin(family);
+      ka<<<grid, block, smem, c.stream>>>(fat, lng, a, fin);
+      timing_end(family);
+      MKS_CUDA(cudaGetLastError());
+      return MKS_OK;
+    }
+  }
   auto kp = k_dslash_p<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin>;
   auto k1 = k_dslash1<R, LinkT, InT, OutT, EPI, NSUM, Fin>;
   auto kd = k_dslash<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin>;
@@ -540,13 +564,17 @@ static int launch_shape(int family, const LinkT &fat, const LinkT &lng,
   const bool pipe = sh.pipe != 0, persist = sh.persist != 0;
   switch (sh.NB) {
   case 1:
-    return launch_dslash_nb<R, LinkT, InT, OutT, 1, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block, pipe, persist);
+    return launch_dslash_nb<R, LinkT, InT, OutT, 1, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block, pipe, persist,
+                                                                   sh.as);
   case 2:
-    return launch_dslash_nb<R, LinkT, InT, OutT, 2, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block, pipe, persist);
+    return launch_dslash_nb<R, LinkT, InT, OutT, 2, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block, pipe, persist,
+                                                                   sh.as);
   case 4:
-    return launch_dslash_nb<R, LinkT, InT, OutT, 4, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block, pipe, persist);
+    return launch_dslash_nb<R, LinkT, InT, OutT, 4, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block, pipe, persist,
+                                                                   sh.as);
   default:
-    return launch_dslash_nb<R, LinkT, InT, OutT, 8, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block, pipe, persist);
+    return launch_dslash_nb<R, LinkT, InT, OutT, 8, EPI, NSUM, Fin>(family, fat, lng, a, fin, sh.block, pipe, persist,
+                                                                   sh.as);
   }
 }
 
@@ -576,6 +604,16 @@ static bool split_epilogue() {
   static int v = -1;
   if (v < 0) {
     const char *e = getenv("MKS_SPLIT_EPI");
+    v = e ? atoi(e) : 1;
+  }
+  return v != 0;
+}
+
+// MKS_ASYNC=0 keeps the cp.async link-prefetch D_eo kernel out of the tuner's candidates
+static bool async_enabled() {
+  static int v = -1;
+  if (v < 0) {
+    const char *e = getenv("MKS_ASYNC");
     v = e ? atoi(e) : 1;
   }
   return v != 0;
@@ -646,10 +684,14 @@ static int tune_shape(const LinkT &fat, const LinkT &lng, int nsrc, Shape *best)
     for (int G = 1; G <= 16; G *= 2) {
       const int NB = nbs[ib];
       if (G * NB < nsrc || G * NB > MAXSRC || (G * NB >= 2 * nsrc && G * NB > 1)) continue;
-      for (int cand = 0; cand < 8; cand++) {
-        const int block = (cand & 1) ? 256 : 128, pipe = (cand >> 1) & 1, persist = cand >> 2;
+      for (int cand = 0; cand < 12; cand++) {
+        // 0-7: block x pipelined x persistent; 8-11: block x cp.async stages 2, 3 (FP32 links)
+        const int block = (cand & 1) ? 256 : 128;
+        const int pipe = cand < 8 ? (cand >> 1) & 1 : 0, persist = cand < 8 ? (cand >> 2) & 1 : 0;
+        const int as = cand < 8 ? 0 : 2 + ((cand >> 1) & 1);
         if ((pipe && !pipe_enabled()) || (pipe && persist)) continue;
-        Shape sh = {G, NB, block, 0, pipe, persist};
+        if (as && (!std::is_same<LinkT, LinkF32>::value || !async_enabled())) continue;
+        Shape sh = {G, NB, block, 0, pipe, persist, as};
         float tot = 0;
         for (int it = 0; it < 4; it++) {
           MKS_CUDA(cudaEventRecord(e0, c.stream));
@@ -723,7 +765,10 @@ static bool shape_override(int prec, int nsrc, bool epi, Shape *out) {
       const size_t f = item.find_first_not_of("0123456789:");
       const std::string flags = f == std::string::npos ? "" : item.substr(f);
       const int pipe = flags.find('p') != std::string::npos, persist = flags.find('g') != std::string::npos;
-      *out = {G, NB, B, 0, pipe, persist};
+      // ":a2" / ":a3": links fetched ahead by cp.async, 2 or 3 buffers (FP32)
+      const size_t fa = flags.find('a');
+      const int as = (fa != std::string::npos && fa + 1 < flags.size()) ? flags[fa + 1] - '0' : 0;
+      *out = {G, NB, B, 0, pipe, persist, (as == 2 || as == 3) && prec == MKS_PREC_SINGLE ? as : 0};
       return true;
     }
     int T, Rr;
@@ -2669,5 +2714,5 @@ extern "C" int mks_tuned_variant(int prec, int nsrc, int epi) {
   if (prec < 0 || prec > 2 || nsrc < 1 || nsrc > MAXSRC) return MKS_ERR_ARG;
   const Shape &s = (epi ? g_shape_epi : g_shape)[prec][nsrc];
   if (s.G == 0) return MKS_ERR_STATE;
-  return (s.tma ? 1 : (s.pipe ? 2 : 0)) + (s.persist ? 4 : 0);
+  return (s.tma ? 1 : (s.pipe ? 2 : (s.as ? 3 : 0))) + (s.persist ? 4 : 0) + 8 * s.as;
 }
