@@ -609,12 +609,15 @@ static bool split_epilogue() {
   return v != 0;
 }
 
-// MKS_ASYNC=0 keeps the cp.async link-prefetch D_eo kernel out of the tuner's candidates
+// MKS_ASYNC=1 adds the cp.async link-prefetch D_eo kernel (k_dslash_a) to the
+// tuner's candidates.  Off by default: measured on GB300 (8 sources,
+// 32^3x64) its D_eo took 350 ms (2 stages) and 415 ms (3 stages) per solve
+// of 8 against 230 ms for k_dslash, and one source 112 against 103 ms.
 static bool async_enabled() {
   static int v = -1;
   if (v < 0) {
     const char *e = getenv("MKS_ASYNC");
-    v = e ? atoi(e) : 1;
+    v = e ? atoi(e) : 0;
   }
   return v != 0;
 }
@@ -738,8 +741,10 @@ static int tune_shape(const LinkT &fat, const LinkT &lng, int nsrc, Shape *best)
 // cache written by the user); entries must satisfy G*NB >= nsrc, G*NB <= 16,
 // NB in {1,2,4,8}, G a power of two, block in {128,256}.  The entry
 // "prec:nsrc:G:1:tma" (prec 1, FP32) selects the TMA-staged kernel with G
-// threads per site, where the lattice admits its tiles.  A leading "d" or
-// "e" limits an entry to the plain D or to the fused-epilogue launches.
+// threads per site, where the lattice admits its tiles.  A trailing ":p"
+// selects the software-pipelined kernel, ":g" the persistent grid, ":a2" or
+// ":a3" the cp.async link buffers (FP32).  A leading "d" or "e" limits an
+// entry to the plain D or to the fused-epilogue launches.
 static bool shape_override(int prec, int nsrc, bool epi, Shape *out) {
   const char *e = getenv("MKS_SHAPE");
   if (!e) return false;
@@ -761,11 +766,9 @@ static bool shape_override(int prec, int nsrc, bool epi, Shape *out) {
     if (sscanf(item.c_str(), "%d:%d:%d:%d:%d", &p, &n, &G, &NB, &B) == 5 && p == prec &&
         n == nsrc && G >= 1 && G <= 16 && (G & (G - 1)) == 0 && (NB == 1 || NB == 2 || NB == 4 || NB == 8) &&
         G * NB >= nsrc && G * NB <= MAXSRC && (B == 128 || B == 256)) {
-      // trailing flags: ":p" the software-pipelined kernel, ":g" a persistent grid
       const size_t f = item.find_first_not_of("0123456789:");
       const std::string flags = f == std::string::npos ? "" : item.substr(f);
       const int pipe = flags.find('p') != std::string::npos, persist = flags.find('g') != std::string::npos;
-      // ":a2" / ":a3": links fetched ahead by cp.async, 2 or 3 buffers (FP32)
       const size_t fa = flags.find('a');
       const int as = (fa != std::string::npos && fa + 1 < flags.size()) ? flags[fa + 1] - '0' : 0;
       *out = {G, NB, B, 0, pipe, persist, (as == 2 || as == 3) && prec == MKS_PREC_SINGLE ? as : 0};

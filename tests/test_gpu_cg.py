@@ -190,6 +190,31 @@ def test_block_cg_tma_staged_links(gpu, oracle_cls, monkeypatch, nsrc):
         assert rel(xs[k], xo) < 1e-7, (k, rel(xs[k], xo))
 
 
+@pytest.mark.parametrize("flags,variant", [("p", 2), ("g", 4), ("a2", 19), ("a3", 27)])
+@pytest.mark.parametrize("nsrc", [3, 8])
+def test_block_cg_variant_kernels(gpu, oracle_cls, monkeypatch, flags, variant, nsrc):
+    """The FP32 multi-source D_eo variants the autotuner can be offered
+    (software-pipelined link loads, persistent grid, cp.async link buffers
+    with 2 or 3 stages), each forced through MKS_SHAPE for both D launches
+    of the iteration: the variant reported in use is the forced one and every
+    source reaches the oracle's solution."""
+    m = gpu
+    dims = (8, 8, 12, 8)
+    NB = 2 if nsrc <= 4 else 4
+    monkeypatch.setenv("MKS_SHAPE", "1:%d:2:%d:256:%s" % (nsrc, NB, flags))
+    m.set_lattice((4, 4, 4, 4))   # a lattice change drops the shapes chosen earlier
+    orc, fat, lng = _setup(m, oracle_cls, dims)
+    srcs = [m.gen_vector(dims, 700 + k, m.ODD) for k in range(nsrc)]
+    xs = [np.zeros_like(s) for s in srcs]
+    qic = m.QuarkInvertControl(resid=1e-10, max=2000, nrestart=5, parity=m.ODD, prec=m.PREC_SINGLE)
+    it, per = m.ks_congrad_block_parity(srcs, xs, qic, 0.05)
+    assert m._lib.load().mks_tuned_variant(m.PREC_SINGLE, nsrc, 0) == variant
+    for k in range(nsrc):
+        assert per[k].converged == 1
+        _, xo, _ = orc.congrad(fat, lng, srcs[k], np.zeros_like(srcs[k]), 0.05, m.ODD, 1e-13, 0.0, 2000, 5)
+        assert rel(xs[k], xo) < 1e-7, (k, rel(xs[k], xo))
+
+
 @pytest.mark.parametrize("parity", ["EVEN", "ODD"])
 def test_block_cg_page_locked_host_arrays(gpu, oracle_cls, parity):
     """Page-locked host arrays are read and written in place by the layout
