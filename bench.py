@@ -540,8 +540,9 @@ def gpu_arm(args):
     def variant(v):
         if v is None or v < 0:
             return None
-        return ["direct loads", "TMA-staged links", "direct loads, pipelined"][v & 3] + \
-            (", persistent grid" if v & 4 else "")
+        kind = ["direct loads", "TMA-staged links", "direct loads, pipelined",
+                "cp.async link buffers x%d" % (v >> 3)][v & 3]
+        return kind + (", persistent grid" if v & 4 else "")
     if lib.mks_tuned_shape(prec, N, ctypes.byref(G), ctypes.byref(nb), ctypes.byref(blk)) == 0:
         shapes["D"] = {"G": G.value, "NB": nb.value, "block": blk.value,
                        "kernel": variant(lib.mks_tuned_variant(prec, N, 0))}
