@@ -622,12 +622,25 @@ static bool async_enabled() {
   return v != 0;
 }
 
-// MKS_PIPE=0 keeps the software-pipelined D_eo kernel out of the tuner's candidates
+// MKS_PIPE=1 and MKS_PERSIST=1 add the software-pipelined (k_dslash_p) and
+// the persistent-grid (k_dslash_g) D_eo kernels to the tuner's candidates.
+// Off by default: on GB300 neither beat k_dslash on a solve (8 sources,
+// 32^3x64: 0.0713-0.0733 and 0.0745-0.0793 against 0.0669 s per source),
+// and every extra candidate costs tuning launches at the first use of each
+// source count (on 48^3x96 a trajectory's tuning took 84 s with both on).
 static bool pipe_enabled() {
   static int v = -1;
   if (v < 0) {
     const char *e = getenv("MKS_PIPE");
-    v = e ? atoi(e) : 1;
+    v = e ? atoi(e) : 0;
+  }
+  return v != 0;
+}
+static bool persist_enabled() {
+  static int v = -1;
+  if (v < 0) {
+    const char *e = getenv("MKS_PERSIST");
+    v = e ? atoi(e) : 0;
   }
   return v != 0;
 }
@@ -681,7 +694,35 @@ static int tune_shape(const LinkT &fat, const LinkT &lng, int nsrc, Shape *best)
   cudaEvent_t e0, e1;
   MKS_CUDA(cudaEventCreate(&e0));
   MKS_CUDA(cudaEventCreate(&e1));
+  // One launch per candidate first; a candidate more than 1.5x slower than
+  // the best average so far is dropped after it, the others are timed over
+  // 3 more launches.  The default shape goes first so that slow candidates
+  // (spilling source counts per thread, wide G) cost one launch each.
   float best_ms = 1e30f;
+  auto time_one = [&](const Shape &sh, float *ms) -> int {
+    MKS_CUDA(cudaEventRecord(e0, c.stream));
+    MKS_TRY((launch_shape<R, LinkT, InT, OutT, EPI, (EPI == EPI_AXPY ? 3 : 0)>(MKS_K_TUNE, fat, lng, a, NoFinish(),
+                                                                                sh)));
+    MKS_CUDA(cudaEventRecord(e1, c.stream));
+    MKS_CUDA(cudaEventSynchronize(e1));
+    MKS_CUDA(cudaEventElapsedTime(ms, e0, e1));
+    return MKS_OK;
+  };
+  auto try_shape = [&](const Shape &sh) -> int {
+    float first, ms, tot = 0;
+    MKS_TRY(time_one(sh, &first));
+    if (sh.tma) MKS_TRY(red_check());
+    if (first > 1.5f * best_ms) return MKS_OK;
+    for (int it = 0; it < 3; it++) {
+      MKS_TRY(time_one(sh, &ms));
+      tot += ms;
+    }
+    if (sh.tma) MKS_TRY(red_check());
+    if (tot / 3 < best_ms) { best_ms = tot / 3; *best = sh; }
+    return MKS_OK;
+  };
+  const Shape def = *best;
+  MKS_TRY(try_shape(def));
   const int nbs[4] = {1, 2, 4, 8};
   for (int ib = 0; ib < 4; ib++) {
     for (int G = 1; G <= 16; G *= 2) {
@@ -692,21 +733,11 @@ static int tune_shape(const LinkT &fat, const LinkT &lng, int nsrc, Shape *best)
         const int block = (cand & 1) ? 256 : 128;
         const int pipe = cand < 8 ? (cand >> 1) & 1 : 0, persist = cand < 8 ? (cand >> 2) & 1 : 0;
         const int as = cand < 8 ? 0 : 2 + ((cand >> 1) & 1);
-        if ((pipe && !pipe_enabled()) || (pipe && persist)) continue;
+        if ((pipe && !pipe_enabled()) || (persist && !persist_enabled()) || (pipe && persist)) continue;
         if (as && (!std::is_same<LinkT, LinkF32>::value || !async_enabled())) continue;
         Shape sh = {G, NB, block, 0, pipe, persist, as};
-        float tot = 0;
-        for (int it = 0; it < 4; it++) {
-          MKS_CUDA(cudaEventRecord(e0, c.stream));
-          MKS_TRY((launch_shape<R, LinkT, InT, OutT, EPI, (EPI == EPI_AXPY ? 3 : 0)>(MKS_K_TUNE, fat, lng, a,
-                                                                                      NoFinish(), sh)));
-          MKS_CUDA(cudaEventRecord(e1, c.stream));
-          MKS_CUDA(cudaEventSynchronize(e1));
-          float ms;
-          MKS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-          if (it > 0) tot += ms;
-        }
-        if (tot < best_ms) { best_ms = tot; *best = sh; }
+        if (memcmp(&sh, &def, sizeof sh) == 0) continue;
+        MKS_TRY(try_shape(sh));
       }
     }
   }
@@ -717,19 +748,7 @@ static int tune_shape(const LinkT &fat, const LinkT &lng, int nsrc, Shape *best)
     int T, Rr;
     if (nsrc >= 2 && !g_tma_off && tma_tile(c.geom, G, &T, &Rr)) {
       Shape sh = {G, 1, T * G, 1};
-      float tot = 0;
-      for (int it = 0; it < 4; it++) {
-        MKS_CUDA(cudaEventRecord(e0, c.stream));
-        MKS_TRY((launch_shape<R, LinkT, InT, OutT, EPI, (EPI == EPI_AXPY ? 3 : 0)>(MKS_K_TUNE, fat, lng, a, NoFinish(),
-                                                                                    sh)));
-        MKS_CUDA(cudaEventRecord(e1, c.stream));
-        MKS_CUDA(cudaEventSynchronize(e1));
-        float ms;
-        MKS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        if (it > 0) tot += ms;
-      }
-      MKS_TRY(red_check());
-      if (tot < best_ms) { best_ms = tot; *best = sh; }
+      MKS_TRY(try_shape(sh));
     }
   }
   cudaEventDestroy(e0);
