@@ -425,6 +425,15 @@ static bool take_tma_retry() {
   return r;
 }
 
+static int tune_class(int nsrc) {
+  return nsrc <= 2 ? nsrc : nsrc <= 4 ? 4 : nsrc <= 8 ? 8 : MAXSRC;
+}
+
+// Tuning launches cover at most this many output sites (the first ones):
+// enough site blocks for many waves on every shape, and on large lattices a
+// fraction of a full launch (a 16-source FP64 D_eo on 48^3x96 takes 80 ms).
+constexpr size_t TUNE_SITES = size_t(1) << 20;
+
 static Shape default_shape(int nsrc) {
   if (nsrc <= 1) return {1, 1, 256, 0, 0};
   if (nsrc <= 2) return {1, 2, 256, 0, 0};
@@ -477,7 +486,8 @@ static int launch_dslash_nb(int family, const LinkT &fat, const LinkT &lng,
                             DslashArgs<InT, OutT, typename EpiLoad<R>::type> &a, const Fin &fin, int block,
                             bool pipe, bool persist, int as = 0) {
   Context &c = ctx();
-  size_t threads = (size_t)c.Vh * a.groups;
+  const size_t sites = family == MKS_K_TUNE && c.Vh > TUNE_SITES ? TUNE_SITES : c.Vh;
+  size_t threads = sites * a.groups;
   const int nvb = (int)((threads + block - 1) / block);
   if constexpr (std::is_same<LinkT, LinkF32>::value) {
     if (as == 2 || as == 3) {
@@ -544,7 +554,7 @@ static int launch_shape(int family, const LinkT &fat, const LinkT &lng,
       Context &c = ctx();
       int T, Rr;
       if (sh.NB != 1 || !tma_tile(a.g, sh.G, &T, &Rr) || a.nsrc > sh.G) return MKS_ERR_ARG;
-      const int grid = (int)(c.Vh / T);
+      const int grid = (int)((family == MKS_K_TUNE && c.Vh > TUNE_SITES ? TUNE_SITES : c.Vh) / T);
       const size_t smem = (size_t)T * 1152;
       static bool attr = false;
       if (!attr) {
@@ -641,6 +651,20 @@ static bool persist_enabled() {
   if (v < 0) {
     const char *e = getenv("MKS_PERSIST");
     v = e ? atoi(e) : 0;
+  }
+  return v != 0;
+}
+
+// The sloppy multi-shift stops when the lowest shift's residual, recomputed
+// in FP64 by a reliable update, meets the target (the iterated residual
+// alone drifts a little above it, and every shift that misses the target
+// then takes a block-CG refinement from a fresh Krylov space).
+// MKS_MS_TRUE_STOP=0 stops on the iterated residual as the FP64 solve does.
+static bool ms_true_stop() {
+  static int v = -1;
+  if (v < 0) {
+    const char *e = getenv("MKS_MS_TRUE_STOP");
+    v = e ? atoi(e) : 1;
   }
   return v != 0;
 }
@@ -809,12 +833,20 @@ template <typename R, class LinkT, class InT, class OutT, int EPI, int NSUM, cla
 static int launch_dslash(int family, const LinkT &fat, const LinkT &lng,
                          DslashArgs<InT, OutT, typename EpiLoad<R>::type> &a, const Fin &fin) {
   const int pk = PrecOf<LinkT>::v;
-  Shape &sh = (EPI == EPI_AXPY ? g_shape_epi : g_shape)[pk][a.nsrc];
+  Shape(&tab)[MAXSRC + 1] = (EPI == EPI_AXPY ? g_shape_epi : g_shape)[pk];
+  Shape &sh = tab[a.nsrc];
   if (sh.G == 0) {
     Shape t;
     if (!shape_override(pk, a.nsrc, EPI == EPI_AXPY, &t)) {
-      if (EPI == EPI_AXPY) MKS_TRY((tune_shape<LinkT, EPI_AXPY>(fat, lng, a.nsrc, &t)));
-      else MKS_TRY(tune_shape(fat, lng, a.nsrc, &t));
+      // source counts are tuned in classes 1, 2, 3-4, 5-8, 9-16: the shape
+      // tuned for a class's widest count serves every count of the class
+      // (the unused source slots of a thread are masked)
+      const int cls = tune_class(a.nsrc);
+      if (tab[cls].G == 0) {
+        if (EPI == EPI_AXPY) MKS_TRY((tune_shape<LinkT, EPI_AXPY>(fat, lng, cls, &tab[cls])));
+        else MKS_TRY(tune_shape(fat, lng, cls, &tab[cls]));
+      }
+      t = tab[cls];
     }
     sh = t;
   }
@@ -1844,7 +1876,8 @@ struct MsState {
   double maxrr, delta;   // reliable updates of the sloppy solve: max |r| since the last one, threshold
   double rsqretire;      // sloppy solve: a shift whose |zeta_j r|^2 fell below this is no longer updated
   int iter, niter, status, j_low, num_now, num_offsets, need_scroll, want_reliable;
-  int n_reliable, pad;
+  int n_reliable;
+  int check_true;        // sloppy solve: stop only when the lowest shift's FP64 residual meets the target
   int retired[MAXSH];
   long long shift_updates;  // sum over iterations of the shifts the update kernel advanced
 };
@@ -1916,6 +1949,9 @@ __device__ __forceinline__ void ms_update(MsState &m, double rsq) {
           if (j != m.j_low && m.zeta_ip1[j] * m.zeta_ip1[j] * m.rsq < m.rsqretire) m.retired[j] = 1;
       if ((m.rsqstop > 0 && m.rsq <= m.rsqstop) || m.iter >= m.niter || !isfinite(m.rsq)) {
         m.status = ST_HOST;
+        // the sloppy recursion met the target: the host recomputes the
+        // lowest shift's residual in FP64 and goes on unless that meets it
+        if (m.check_true && m.delta > 0 && m.iter < m.niter && isfinite(m.rsq)) m.want_reliable = 1;
       } else if (m.delta > 0) {
         // sloppy solve: ask for a reliable update when |r| fell below
         // delta * max|r| since the last one
@@ -2202,6 +2238,7 @@ static int multishift_core(const LinkSlot &sl, int par, int prec, const double2 
     // sloppy solve: stop updating a shift once its iterated residual is a
     // decade below the target (its true residual is checked afterwards)
     h.rsqretire = h.delta > 0 ? 0.01 * h.rsqstop : 0.0;
+    h.check_true = h.delta > 0 && ms_true_stop();
   }
   if (h.delta > 0)
     for (int j = 0; j < nsh; j++) MKS_CUDA(cudaMemsetAsync(x64[j], 0, n * sizeof(double2), c.stream));
@@ -2371,6 +2408,7 @@ static int multishift_multi_core(const LinkSlot &sl, int par, int nf, const doub
     h.maxrr = sqrt(sn);
     h.delta = delta;
     h.rsqretire = 0.01 * h.rsqstop;
+    h.check_true = ms_true_stop();
     for (int j = 0; j < nsh[f]; j++) MKS_CUDA(cudaMemsetAsync(x64[f][j], 0, n * sizeof(double2), c.stream));
   }
   MKS_CUDA(cudaMemcpyAsync(st, hs, nf * sizeof(MsState), cudaMemcpyHostToDevice, c.stream));
