@@ -669,6 +669,17 @@ static bool ms_true_stop() {
   return v != 0;
 }
 
+// MKS_MS_SHIFT64=1: the sloppy single-field multi-shift keeps the shifts'
+// search directions and solutions in FP64 (FP32 residual and D_eo)
+static bool ms_shift64() {
+  static int v = -1;
+  if (v < 0) {
+    const char *e = getenv("MKS_MS_SHIFT64");
+    v = e ? atoi(e) : 0;
+  }
+  return v != 0;
+}
+
 static void set_vec(VecF64 &v, float *p, float *) { v.p = (double2 *)p; }
 static void set_vec(VecF32 &v, float *p, float *) { v.p = (float2 *)p; }
 static void set_vec(VecF16 &v, float *p, float *n) { v.p = (__half2 *)p; v.norm = n; }
@@ -1538,7 +1549,20 @@ static int congrad_block_dev(int nsrc, const double *const *src_dev, double *con
 // The device address of a page-locked host array mapped into the device
 // address space (cudaHostAlloc / cudaHostRegister), else nullptr (pageable
 // memory, which kernels must not touch).
+// MKS_HOST_INPLACE=0 copies page-locked host fields in and out with the
+// copy engines (cudaMemcpyAsync) like pageable ones, instead of reading and
+// writing them in place from the layout kernels
+static bool host_inplace() {
+  static int v = -1;
+  if (v < 0) {
+    const char *e = getenv("MKS_HOST_INPLACE");
+    v = e ? atoi(e) : 1;
+  }
+  return v != 0;
+}
+
 static double *mapped_host(const double *p) {
+  if (!host_inplace()) return nullptr;
   cudaPointerAttributes at;
   if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
     cudaGetLastError();
@@ -2000,12 +2024,13 @@ struct FinMsUpdateM {
 
 // K3 at one site for one field: r += beta ttt, every shift's psim and pm,
 // the lowest shift's p (and its FP16 shadow); out[0] = |r|^2 at the site
-template <typename R>
-__device__ __forceinline__ void ms_site_update(const MsState &m, typename VT<R>::v2 *const *psim,
-                                               typename VT<R>::v2 *const *pm, typename VT<R>::v2 *r,
+template <typename R, typename RS = R>
+__device__ __forceinline__ void ms_site_update(const MsState &m, typename VT<RS>::v2 *const *psim,
+                                               typename VT<RS>::v2 *const *pm, typename VT<R>::v2 *r,
                                                const typename VT<R>::v2 *ttt, typename VT<R>::v2 *cgp,
                                                __half2 *p16, float *p16n, int h, int Vh, double *out) {
     typedef typename VT<R>::v2 T2;
+    typedef typename VT<RS>::v2 S2;
     const int n = m.num_now, jl = m.j_low;
     const R bl = (R)m.beta_i[jl];
     T2 rn[3];
@@ -2021,29 +2046,29 @@ __device__ __forceinline__ void ms_site_update(const MsState &m, typename VT<R>:
     }
     for (int j = 0; j < n; j++) {
       if (m.retired[j]) continue;
-      const R bj = (R)m.beta_i[j], zj = (R)m.zeta_ip1[j], aj = (R)m.alpha[j];
+      const RS bj = (RS)m.beta_i[j], zj = (RS)m.zeta_ip1[j], aj = (RS)m.alpha[j];
 #pragma unroll
       for (int k = 0; k < 3; k++) {
         size_t i = (size_t)k * Vh + h;
-        T2 pv = pm[j][i], xv = psim[j][i];
+        S2 pv = pm[j][i], xv = psim[j][i];
         xv.x = xv.x + bj * pv.x; xv.y = xv.y + bj * pv.y;
-        pv.x = zj * rn[k].x + aj * pv.x; pv.y = zj * rn[k].y + aj * pv.y;
+        pv.x = zj * (RS)rn[k].x + aj * pv.x; pv.y = zj * (RS)rn[k].y + aj * pv.y;
         psim[j][i] = xv;
         pm[j][i] = pv;
-        if (j == jl) cgp[i] = pv;
+        if (j == jl) { T2 cv; cv.x = (R)pv.x; cv.y = (R)pv.y; cgp[i] = cv; }
       }
       if (j == jl && p16) {
         float mx = 0.f;
 #pragma unroll
         for (int k = 0; k < 3; k++) {
-          T2 pv = pm[j][(size_t)k * Vh + h];
+          S2 pv = pm[j][(size_t)k * Vh + h];
           mx = fmaxf(mx, fmaxf(fabsf((float)pv.x), fabsf((float)pv.y)));
         }
         float inv = mx > 0.f ? 1.f / mx : 0.f;
         p16n[h] = mx;
 #pragma unroll
         for (int k = 0; k < 3; k++) {
-          T2 pv = pm[j][(size_t)k * Vh + h];
+          S2 pv = pm[j][(size_t)k * Vh + h];
           p16[(size_t)k * Vh + h] = __floats2half2_rn((float)pv.x * inv, (float)pv.y * inv);
         }
       }
@@ -2051,16 +2076,17 @@ __device__ __forceinline__ void ms_site_update(const MsState &m, typename VT<R>:
     out[0] = rr;
 }
 
-template <typename R> struct OpShiftUpdate {
+template <typename R, typename RS = R> struct OpShiftUpdate {
   typedef typename VT<R>::v2 T2;
-  T2 *psim[MAXSH], *pm[MAXSH];
+  typedef typename VT<RS>::v2 S2;
+  S2 *psim[MAXSH], *pm[MAXSH];
   T2 *r, *ttt, *cgp;
   __half2 *p16;
   float *p16n;
   const MsState *st;
   int Vh;
   __device__ void operator()(int h, int, double *out) const {
-    ms_site_update<R>(*st, psim, pm, r, ttt, cgp, p16, p16n, h, Vh, out);
+    ms_site_update<R, RS>(*st, psim, pm, r, ttt, cgp, p16, p16n, h, Vh, out);
   }
 };
 
@@ -2079,9 +2105,10 @@ template <typename R> struct OpShiftUpdateM {
 };
 
 // initial fields: r = p = pm_j = src (converted), psim_j = 0
-template <typename R> struct OpShiftInit {
+template <typename R, typename RS = R> struct OpShiftInit {
   typedef typename VT<R>::v2 T2;
-  T2 *psim[MAXSH], *pm[MAXSH];
+  typedef typename VT<RS>::v2 S2;
+  S2 *psim[MAXSH], *pm[MAXSH];
   T2 *r, *cgp;
   const double2 *src;
   __half2 *p16;
@@ -2100,8 +2127,9 @@ template <typename R> struct OpShiftInit {
       a += sv.x * sv.x + sv.y * sv.y;
       mx = fmaxf(mx, fmaxf(fabsf((float)sv.x), fabsf((float)sv.y)));
       for (int j = 0; j < n; j++) {
-        pm[j][i] = v[k];
-        T2 z; z.x = 0; z.y = 0;
+        S2 pv; pv.x = (RS)sv.x; pv.y = (RS)sv.y;
+        pm[j][i] = pv;
+        S2 z; z.x = 0; z.y = 0;
         psim[j][i] = z;
       }
     }
@@ -2174,23 +2202,33 @@ static int ms_fold(int nsh, double2 *const *x64, void *const *x32) {
 // residual of the lowest shift is recomputed in FP64 from x64_low and
 // replaces the sloppy one (the shifted residuals stay zeta_j r); on exit
 // x64_j holds the whole solution.
-template <typename R>
+// RS: storage of the shifts' solutions and search directions.  RS = double
+// with R = float keeps p_j and x_j in FP64 (the solutions are then the x64
+// accumulators themselves, no fold): the shifted residuals zeta_j r stay
+// consistent with the shifts' solutions, which FP32 p_j and x_j lose to
+// rounding that the lowest shift's reliable updates do not repair.
+template <typename R, typename RS = R>
 static int multishift_core(const LinkSlot &sl, int par, int prec, const double2 *src64, int nsh,
                            const double *offsets, double resid, int niter, void **psim_out, MsState *hstate,
                            double2 *const *x64 = nullptr, double delta = 0.0) {
   typedef typename VT<R>::v2 T2;
+  typedef typename VT<RS>::v2 S2;
+  constexpr bool wide = !std::is_same<R, RS>::value;
   Context &c = ctx();
   const int Vh = (int)c.Vh;
   size_t n = 3 * c.Vh;
-  T2 *r, *cgp, *ttt, *t, *pm[MAXSH], *psim[MAXSH];
+  T2 *r, *cgp, *ttt, *t;
+  S2 *pm[MAXSH], *psim[MAXSH];
   const char *tag = sizeof(R) == 8 ? "64" : "32";
+  const char *stag = sizeof(RS) == 8 ? "64" : "32";
   MKS_TRY(wsv(std::string("ms_r") + tag, n, &r));
   MKS_TRY(wsv(std::string("ms_p") + tag, n, &cgp));
   MKS_TRY(wsv(std::string("ms_ttt") + tag, n, &ttt));
   MKS_TRY(wsv(std::string("ms_t") + tag, n, &t));
   for (int j = 0; j < nsh; j++) {
-    MKS_TRY(wsv(std::string("ms_pm") + tag + "_" + std::to_string(j), n, &pm[j]));
-    MKS_TRY(wsv(std::string("ms_x") + tag + "_" + std::to_string(j), n, &psim[j]));
+    MKS_TRY(wsv(std::string("ms_pm") + stag + "_" + std::to_string(j), n, &pm[j]));
+    if (wide && x64) psim[j] = (S2 *)x64[j];
+    else MKS_TRY(wsv(std::string("ms_x") + stag + "_" + std::to_string(j), n, &psim[j]));
     psim_out[j] = psim[j];
   }
   __half2 *p16 = nullptr, *t16 = nullptr;
@@ -2218,13 +2256,13 @@ static int multishift_core(const LinkSlot &sl, int par, int prec, const double2 
   h.j_low = j_low; h.num_now = nsh; h.num_offsets = nsh; h.niter = niter;
   for (int j = 0; j < nsh; j++) { h.zeta_im1[j] = h.zeta_i[j] = 1.0; h.beta_im1[j] = -1.0; h.alpha[j] = 0.0; }
   {
-    OpShiftInit<R> op;
+    OpShiftInit<R, RS> op;
     memset(&op, 0, sizeof op);
     for (int j = 0; j < nsh; j++) { op.psim[j] = psim[j]; op.pm[j] = pm[j]; }
     op.r = r; op.cgp = cgp; op.src = src64; op.p16 = p16; op.p16n = p16n; op.Vh = Vh; op.n = nsh;
     double *tot;
     MKS_TRY(wsv("ms_tot", 4, &tot));
-    MKS_TRY((launch_site<OpShiftInit<R>, 1, FinNone>(MKS_K_BLAS, op, FinNone(), nullptr, 1, tot)));
+    MKS_TRY((launch_site<OpShiftInit<R, RS>, 1, FinNone>(MKS_K_BLAS, op, FinNone(), nullptr, 1, tot)));
     double sn = 0;
     MKS_CUDA(cudaMemcpyAsync(&sn, tot, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     MKS_CUDA(cudaStreamSynchronize(c.stream));
@@ -2240,7 +2278,7 @@ static int multishift_core(const LinkSlot &sl, int par, int prec, const double2 
     h.rsqretire = h.delta > 0 ? 0.01 * h.rsqstop : 0.0;
     h.check_true = h.delta > 0 && ms_true_stop();
   }
-  if (h.delta > 0)
+  if (h.delta > 0 && !wide)
     for (int j = 0; j < nsh; j++) MKS_CUDA(cudaMemsetAsync(x64[j], 0, n * sizeof(double2), c.stream));
   MKS_CUDA(cudaMemcpyAsync(st, &h, sizeof h, cudaMemcpyHostToDevice, c.stream));
   int zero = 0;
@@ -2292,11 +2330,11 @@ static int multishift_core(const LinkSlot &sl, int par, int prec, const double2 
         a2.r[0].p = (float2 *)r; a2.coef[0] = h.shift0;
         MKS_TRY((launch_dslash<float, LinkF16, VecF16, VecF32, EPI_AXPY, 3>(MKS_K_DSLASH_F16, L.fat, L.lng, a2, FinMsAlpha{st})));
       }
-      OpShiftUpdate<R> up;
+      OpShiftUpdate<R, RS> up;
       memset(&up, 0, sizeof up);
       for (int j = 0; j < nsh; j++) { up.psim[j] = psim[j]; up.pm[j] = pm[j]; }
       up.r = r; up.ttt = ttt; up.cgp = cgp; up.p16 = p16; up.p16n = p16n; up.st = st; up.Vh = Vh;
-      MKS_TRY((launch_site<OpShiftUpdate<R>, 1, FinMsUpdate>(MKS_K_SHIFT, up, FinMsUpdate{st, skip}, skip, 1)));
+      MKS_TRY((launch_site<OpShiftUpdate<R, RS>, 1, FinMsUpdate>(MKS_K_SHIFT, up, FinMsUpdate{st, skip}, skip, 1)));
     }
     return MKS_OK;
   };
@@ -2318,7 +2356,7 @@ static int multishift_core(const LinkSlot &sl, int par, int prec, const double2 
     if (++guard > 10000000) return MKS_ERR_TIMEOUT;
     if (h.status == ST_HOST && h.want_reliable) {
       // reliable update: fold, FP64 residual of the lowest shift, continue
-      MKS_TRY(ms_fold(nsh, x64, psim_out));
+      if (!wide) MKS_TRY(ms_fold(nsh, x64, psim_out));
       double2 *t64, *dd64;
       MKS_TRY(wsv("ms_rel_t64", n, &t64));
       MKS_TRY(wsv("ms_rel_dd64", n, &dd64));
@@ -2339,7 +2377,7 @@ static int multishift_core(const LinkSlot &sl, int par, int prec, const double2 
       MKS_CUDA(cudaMemcpyAsync(skip, &zero, sizeof zero, cudaMemcpyHostToDevice, c.stream));
     }
   }
-  if (h.delta > 0) MKS_TRY(ms_fold(nsh, x64, psim_out));
+  if (h.delta > 0 && !wide) MKS_TRY(ms_fold(nsh, x64, psim_out));
   *hstate = h;
   return MKS_OK;
 }
@@ -2620,8 +2658,12 @@ static int multishift_dev_once(const double *src_dev, double *const *psim_dev, c
   // (generic_ks/ks_multicg.c:170-228)
   double2 *x64[MAXSH];
   for (int j = 0; j < nsh; j++) MKS_TRY(wsv("ms_x64_" + std::to_string(j), 3 * c.Vh, &x64[j]));
-  MKS_TRY(multishift_core<float>(sl, par, arg->prec, src64, nsh, offsets, arg->resid, niter, psim, &h, x64,
-                                 arg->delta > 0 ? arg->delta : 0.1));
+  if (ms_shift64())
+    MKS_TRY((multishift_core<float, double>(sl, par, arg->prec, src64, nsh, offsets, arg->resid, niter, psim, &h,
+                                            x64, arg->delta > 0 ? arg->delta : 0.1)));
+  else
+    MKS_TRY(multishift_core<float>(sl, par, arg->prec, src64, nsh, offsets, arg->resid, niter, psim, &h, x64,
+                                   arg->delta > 0 ? arg->delta : 0.1));
   int total_iters = h.iter;
   g_ms_iters = h.iter;
   g_ms_shift_updates = h.shift_updates;
