@@ -484,12 +484,14 @@ def gpu_arm(args):
     arg64 = _lib.InvertArg(1000, 10, m.EVEN, m.PREC_DOUBLE, RESID, 0.0, 0.1)
     res64 = _lib.InvertResult()
     d64 = torch.zeros_like(d_src[0])
-    torch.cuda.synchronize()
-    t0 = time.time()
-    it64 = m.check(lib.mks_ks_congrad_parity_dev(d_src[0].data_ptr(), d64.data_ptr(), MASS, 0,
-                                                 ctypes.byref(arg64), ctypes.byref(res64)), "fp64 solve")
-    torch.cuda.synchronize()
-    t_fp64 = time.time() - t0
+    for rep in range(2):  # the first call tunes the FP64 D_eo shape and captures the graphs
+        d64.zero_()
+        torch.cuda.synchronize()
+        t0 = time.time()
+        it64 = m.check(lib.mks_ks_congrad_parity_dev(d_src[0].data_ptr(), d64.data_ptr(), MASS, 0,
+                                                     ctypes.byref(arg64), ctypes.byref(res64)), "fp64 solve")
+        torch.cuda.synchronize()
+        t_fp64 = time.time() - t0
 
     for _ in range(args.warmup):
         solve_dev()

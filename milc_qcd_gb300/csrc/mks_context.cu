@@ -162,20 +162,36 @@ int red_check() {
 }
 
 // ---------------- layout conversion kernels ----------------
-// full AoS vector field [V][6] -> one parity SoA double2 [3][Vh]
+// full AoS vector field [V][6] -> one parity SoA double2 [3][Vh].  One
+// complex number per thread: the parity half of a MILC field is 3*Vh
+// consecutive complex numbers, taken in order, so the reads (and in
+// k_vec_soa_to_aos the writes) of the AoS side are contiguous across a warp
+// -- the AoS side is often a page-locked host array read over the host link.
+// 16-byte accesses where the array allows them.
+__device__ __forceinline__ double2 aos_get(const double *base, size_t t) {
+  if (((uintptr_t)base & 15) == 0) return reinterpret_cast<const double2 *>(base)[t];
+  return make_double2(base[2 * t], base[2 * t + 1]);
+}
 __global__ void k_vec_aos_to_soa(const double *__restrict__ aos, double2 *__restrict__ soa, int par, int Vh) {
-  int h = blockIdx.x * blockDim.x + threadIdx.x;
-  if (h >= Vh) return;
-  const double *s = aos + ((size_t)par * Vh + h) * 6;
-#pragma unroll
-  for (int c = 0; c < 3; c++) soa[(size_t)c * Vh + h] = make_double2(s[2 * c], s[2 * c + 1]);
+  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= 3 * (size_t)Vh) return;
+  const size_t h = t / 3;
+  const int c = (int)(t - 3 * h);
+  soa[(size_t)c * Vh + h] = aos_get(aos + (size_t)par * Vh * 6, t);
 }
 __global__ void k_vec_soa_to_aos(const double2 *__restrict__ soa, double *__restrict__ aos, int par, int Vh) {
-  int h = blockIdx.x * blockDim.x + threadIdx.x;
-  if (h >= Vh) return;
-  double *d = aos + ((size_t)par * Vh + h) * 6;
-#pragma unroll
-  for (int c = 0; c < 3; c++) { double2 v = soa[(size_t)c * Vh + h]; d[2 * c] = v.x; d[2 * c + 1] = v.y; }
+  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= 3 * (size_t)Vh) return;
+  const size_t h = t / 3;
+  const int c = (int)(t - 3 * h);
+  const double2 v = soa[(size_t)c * Vh + h];
+  double *base = aos + (size_t)par * Vh * 6;
+  if (((uintptr_t)base & 15) == 0) {
+    reinterpret_cast<double2 *>(base)[t] = v;
+  } else {
+    base[2 * t] = v.x;
+    base[2 * t + 1] = v.y;
+  }
 }
 // links [V][4][18] -> [2][4][9][Vh]
 __global__ void k_links_aos_to_soa(const double *__restrict__ aos, double2 *__restrict__ soa, int Vh) {
@@ -244,22 +260,23 @@ __global__ void k_links_to_f16(const double2 *__restrict__ src, uint4 *__restric
 int vec_aos_to_soa64(const double *aos_dev, double2 *soa, int par) {
   Context &c = g_ctx;
   int Vh = (int)c.Vh;
-  k_vec_aos_to_soa<<<grid_for(Vh, 256), 256, 0, c.stream>>>(aos_dev, soa, par, Vh);
+  k_vec_aos_to_soa<<<grid_for(3 * Vh, 256), 256, 0, c.stream>>>(aos_dev, soa, par, Vh);
   c.launches++;
   MKS_CUDA(cudaGetLastError());
   return MKS_OK;
 }
 __global__ void k_vec_aos_to_soa32(const double *__restrict__ aos, float2 *__restrict__ soa, int par, int Vh) {
-  int h = blockIdx.x * blockDim.x + threadIdx.x;
-  if (h >= Vh) return;
-  const double *s = aos + ((size_t)par * Vh + h) * 6;
-#pragma unroll
-  for (int c = 0; c < 3; c++) soa[(size_t)c * Vh + h] = make_float2((float)s[2 * c], (float)s[2 * c + 1]);
+  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= 3 * (size_t)Vh) return;
+  const size_t h = t / 3;
+  const int c = (int)(t - 3 * h);
+  const double2 v = aos_get(aos + (size_t)par * Vh * 6, t);
+  soa[(size_t)c * Vh + h] = make_float2((float)v.x, (float)v.y);
 }
 int vec_aos_to_soa32(const double *aos_dev, float2 *soa, int par) {
   Context &c = g_ctx;
   int Vh = (int)c.Vh;
-  k_vec_aos_to_soa32<<<grid_for(Vh, 256), 256, 0, c.stream>>>(aos_dev, soa, par, Vh);
+  k_vec_aos_to_soa32<<<grid_for(3 * Vh, 256), 256, 0, c.stream>>>(aos_dev, soa, par, Vh);
   c.launches++;
   MKS_CUDA(cudaGetLastError());
   return MKS_OK;
@@ -267,7 +284,7 @@ int vec_aos_to_soa32(const double *aos_dev, float2 *soa, int par) {
 int vec_soa64_to_aos(const double2 *soa, double *aos_dev, int par) {
   Context &c = g_ctx;
   int Vh = (int)c.Vh;
-  k_vec_soa_to_aos<<<grid_for(Vh, 256), 256, 0, c.stream>>>(soa, aos_dev, par, Vh);
+  k_vec_soa_to_aos<<<grid_for(3 * Vh, 256), 256, 0, c.stream>>>(soa, aos_dev, par, Vh);
   c.launches++;
   MKS_CUDA(cudaGetLastError());
   return MKS_OK;
