@@ -669,13 +669,18 @@ static bool ms_true_stop() {
   return v != 0;
 }
 
-// MKS_MS_SHIFT64=1: the sloppy single-field multi-shift keeps the shifts'
-// search directions and solutions in FP64 (FP32 residual and D_eo)
+// The sloppy multi-shift keeps the shifts' search directions p_j and
+// solutions x_j in FP64 (residual, D_eo and the lowest shift's D_eo input
+// in FP32).  Measured on GB300 (11 offsets, 32^3x64, 1e-10): 0.431 against
+// 0.450 s -- the update kernel moves twice the bytes per shift, but fewer
+// shifts miss the target after the sloppy phase and the block-CG refinement
+// that follows shrinks (330 against 353 iterations for the slowest shift).
+// MKS_MS_SHIFT64=0 stores them in FP32.
 static bool ms_shift64() {
   static int v = -1;
   if (v < 0) {
     const char *e = getenv("MKS_MS_SHIFT64");
-    v = e ? atoi(e) : 0;
+    v = e ? atoi(e) : 1;
   }
   return v != 0;
 }
@@ -2091,16 +2096,17 @@ template <typename R, typename RS = R> struct OpShiftUpdate {
 };
 
 // the same for several fields, one per row k (field map[k])
-template <typename R> struct OpShiftUpdateM {
+template <typename R, typename RS = R> struct OpShiftUpdateM {
   typedef typename VT<R>::v2 T2;
-  T2 *psim[MSF][MAXSH], *pm[MSF][MAXSH];
+  typedef typename VT<RS>::v2 S2;
+  S2 *psim[MSF][MAXSH], *pm[MSF][MAXSH];
   T2 *r[MSF], *ttt[MSF], *cgp[MSF];
   const MsState *st;
   int map[MSF];
   int Vh;
   __device__ void operator()(int h, int k, double *out) const {
     const int f = map[k];
-    ms_site_update<R>(st[f], psim[f], pm[f], r[f], ttt[f], cgp[f], nullptr, nullptr, h, Vh, out);
+    ms_site_update<R, RS>(st[f], psim[f], pm[f], r[f], ttt[f], cgp[f], nullptr, nullptr, h, Vh, out);
   }
 };
 
@@ -2389,14 +2395,18 @@ static int multishift_core(const LinkSlot &sl, int par, int prec, const double2 
 // field's lowest shift, exactly as multishift_core does for one field; a
 // field that stops leaves the launches (the kernels are rebuilt for the
 // remaining fields).  On exit x64[f][j] holds every field's solutions.
+template <typename RS = float>
 static int multishift_multi_core(const LinkSlot &sl, int par, int nf, const double2 *const *src64, const int *nsh,
                                  const double *const *offsets, double resid, int niter, double2 *const *const *x64,
                                  double delta, MsState *hs) {
   typedef float2 T2;
+  typedef typename VT<RS>::v2 S2;
+  constexpr bool wide = sizeof(RS) == 8;
   Context &c = ctx();
   const int Vh = (int)c.Vh;
   const size_t n = 3 * c.Vh;
-  T2 *r[MSF], *cgp[MSF], *ttt[MSF], *t[MSF], *pm[MSF][MAXSH], *psim[MSF][MAXSH];
+  T2 *r[MSF], *cgp[MSF], *ttt[MSF], *t[MSF];
+  S2 *pm[MSF][MAXSH], *psim[MSF][MAXSH];
   for (int f = 0; f < nf; f++) {
     const std::string k = std::to_string(f);
     MKS_TRY(wsv("msm_r_" + k, n, &r[f]));
@@ -2404,8 +2414,9 @@ static int multishift_multi_core(const LinkSlot &sl, int par, int nf, const doub
     MKS_TRY(wsv("msm_ttt_" + k, n, &ttt[f]));
     MKS_TRY(wsv("msm_t_" + k, n, &t[f]));
     for (int j = 0; j < nsh[f]; j++) {
-      MKS_TRY(wsv("msm_pm_" + k + "_" + std::to_string(j), n, &pm[f][j]));
-      MKS_TRY(wsv("msm_x_" + k + "_" + std::to_string(j), n, &psim[f][j]));
+      MKS_TRY(wsv((wide ? "msm_pm64_" : "msm_pm_") + k + "_" + std::to_string(j), n, &pm[f][j]));
+      if (wide) psim[f][j] = (S2 *)x64[f][j];
+      else MKS_TRY(wsv("msm_x_" + k + "_" + std::to_string(j), n, &psim[f][j]));
     }
   }
   MsState *st;
@@ -2430,11 +2441,11 @@ static int multishift_multi_core(const LinkSlot &sl, int par, int nf, const doub
     h.shift0 = -h.shifts[j_low];
     h.j_low = j_low; h.num_now = nsh[f]; h.num_offsets = nsh[f]; h.niter = niter;
     for (int j = 0; j < nsh[f]; j++) { h.zeta_im1[j] = h.zeta_i[j] = 1.0; h.beta_im1[j] = -1.0; h.alpha[j] = 0.0; }
-    OpShiftInit<float> op;
+    OpShiftInit<float, RS> op;
     memset(&op, 0, sizeof op);
     for (int j = 0; j < nsh[f]; j++) { op.psim[j] = psim[f][j]; op.pm[j] = pm[f][j]; }
     op.r = r[f]; op.cgp = cgp[f]; op.src = src64[f]; op.Vh = Vh; op.n = nsh[f];
-    MKS_TRY((launch_site<OpShiftInit<float>, 1, FinNone>(MKS_K_BLAS, op, FinNone(), nullptr, 1, tot1)));
+    MKS_TRY((launch_site<OpShiftInit<float, RS>, 1, FinNone>(MKS_K_BLAS, op, FinNone(), nullptr, 1, tot1)));
     double sn = 0;
     MKS_CUDA(cudaMemcpyAsync(&sn, tot1, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     MKS_CUDA(cudaStreamSynchronize(c.stream));
@@ -2447,7 +2458,8 @@ static int multishift_multi_core(const LinkSlot &sl, int par, int nf, const doub
     h.delta = delta;
     h.rsqretire = 0.01 * h.rsqstop;
     h.check_true = ms_true_stop();
-    for (int j = 0; j < nsh[f]; j++) MKS_CUDA(cudaMemsetAsync(x64[f][j], 0, n * sizeof(double2), c.stream));
+    if (!wide)
+      for (int j = 0; j < nsh[f]; j++) MKS_CUDA(cudaMemsetAsync(x64[f][j], 0, n * sizeof(double2), c.stream));
   }
   MKS_CUDA(cudaMemcpyAsync(st, hs, nf * sizeof(MsState), cudaMemcpyHostToDevice, c.stream));
   const int zero = 0;
@@ -2479,7 +2491,7 @@ static int multishift_multi_core(const LinkSlot &sl, int par, int nf, const doub
           fa.map[q] = f;
         }
         MKS_TRY((launch_dslash<float, LinkF32, VecF32, VecF32, EPI_AXPY, 3>(MKS_K_DSLASH_F32, L.fat, L.lng, a2, fa)));
-        OpShiftUpdateM<float> up;
+        OpShiftUpdateM<float, RS> up;
         memset(&up, 0, sizeof up);
         FinMsUpdateM fu;
         fu.st = st; fu.skip = skip;
@@ -2489,7 +2501,7 @@ static int multishift_multi_core(const LinkSlot &sl, int par, int nf, const doub
         }
         for (int q = 0; q < nact; q++) { up.map[q] = act[q]; fu.map[q] = act[q]; }
         up.st = st; up.Vh = Vh;
-        MKS_TRY((launch_site<OpShiftUpdateM<float>, 1, FinMsUpdateM>(MKS_K_SHIFT, up, fu, skip, nact)));
+        MKS_TRY((launch_site<OpShiftUpdateM<float, RS>, 1, FinMsUpdateM>(MKS_K_SHIFT, up, fu, skip, nact)));
       }
       return MKS_OK;
     };
@@ -2521,7 +2533,7 @@ static int multishift_multi_core(const LinkSlot &sl, int par, int nf, const doub
       MsState &h = hs[f];
       if (h.status != ST_HOST || !h.want_reliable) continue;   // stopped fields leave the launches
       // reliable update of field f: fold, FP64 residual of its lowest shift
-      MKS_TRY(ms_fold(nsh[f], x64[f], (void *const *)psim[f]));
+      if (!wide) MKS_TRY(ms_fold(nsh[f], x64[f], (void *const *)psim[f]));
       double2 *t64, *dd64;
       MKS_TRY(wsv("ms_rel_t64", n, &t64));
       MKS_TRY(wsv("ms_rel_dd64", n, &dd64));
@@ -2542,7 +2554,8 @@ static int multishift_multi_core(const LinkSlot &sl, int par, int nf, const doub
     MKS_CUDA(cudaMemcpyAsync(st, hs, nf * sizeof(MsState), cudaMemcpyHostToDevice, c.stream));
     MKS_CUDA(cudaMemcpyAsync(skip, &zero, sizeof zero, cudaMemcpyHostToDevice, c.stream));
   }
-  for (int f = 0; f < nf; f++) MKS_TRY(ms_fold(nsh[f], x64[f], (void *const *)psim[f]));
+  if (!wide)
+    for (int f = 0; f < nf; f++) MKS_TRY(ms_fold(nsh[f], x64[f], (void *const *)psim[f]));
   MKS_CUDA(cudaStreamSynchronize(c.stream));
   return MKS_OK;
 }
@@ -2580,8 +2593,12 @@ static int multishift_multi_dev_once(int nf, const double *const *src_dev, const
     x64p[f] = x64s[f];
   }
   MsState hs[MSF];
-  MKS_TRY(multishift_multi_core(sl, par, nf, src64, num_offsets, offs, arg->resid, arg->max * arg->nrestart, x64p,
-                                arg->delta > 0 ? arg->delta : 0.1, hs));
+  if (ms_shift64())
+    MKS_TRY(multishift_multi_core<double>(sl, par, nf, src64, num_offsets, offs, arg->resid, arg->max * arg->nrestart,
+                                          x64p, arg->delta > 0 ? arg->delta : 0.1, hs));
+  else
+    MKS_TRY(multishift_multi_core<float>(sl, par, nf, src64, num_offsets, offs, arg->resid, arg->max * arg->nrestart,
+                                         x64p, arg->delta > 0 ? arg->delta : 0.1, hs));
   g_ms_iters = 0;
   g_ms_shift_updates = 0;
   for (int f = 0; f < nf; f++) {
