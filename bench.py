@@ -380,14 +380,20 @@ def extras(m, lib, _lib, torch, srcs):
         # kernel (OpShiftUpdate) and the single-source D_eo pair
         n_it, n_upd = ctypes.c_longlong(), ctypes.c_longlong()
         lib.mks_multishift_counts(ctypes.byref(n_it), ctypes.byref(n_upd))
-        vb = {m.PREC_DOUBLE: 48, m.PREC_SINGLE: 24, m.PREC_HALF: 24}[prec]  # update-kernel vectors
+        # update-kernel vectors: r (read, write), ttt (read) and the lowest
+        # shift's D_eo input (write) in the residual's precision; p_j and x_j
+        # (read, write) of every shift advanced, in FP64 for targets below
+        # 1e-7 (the library's choice unless MKS_MS_SHIFT64 forces one)
+        vb = 48 if prec == m.PREC_DOUBLE else 24
+        force64 = os.environ.get("MKS_MS_SHIFT64")
+        vs = 48 if (prec == m.PREC_DOUBLE or (force64 != "0" and (force64 == "1" or RESID < 1e-7))) else 24
         if "shift" in fam and fam["shift"]["launches"]:
-            upd_bytes = (4 * n_it.value + 4 * n_upd.value) * vb * Vh
+            upd_bytes = (4 * n_it.value * vb + 4 * n_upd.value * vs) * Vh
             gbs = upd_bytes / (fam["shift"]["ms"] * 1e-3) / 1e9
             ms[name]["roofline_shift_update"] = {
                 "bytes": upd_bytes, "ms": fam["shift"]["ms"], "gbs": gbs, "frac": gbs / peak,
-                "per_site": "(4 + 4 x shifts advanced) vectors of %d B per iteration; %d iterations, %d shift "
-                            "updates" % (vb, n_it.value, n_upd.value)}
+                "per_site": "4 vectors of %d B + 4 x shifts advanced vectors of %d B per iteration; %d iterations, "
+                            "%d shift updates" % (vb, vs, n_it.value, n_upd.value)}
         dfam = {m.PREC_DOUBLE: "dslash_f64", m.PREC_SINGLE: "dslash_f32", m.PREC_HALF: "dslash_f16"}[prec]
         if prec != m.PREC_DOUBLE and dfam in fam and fam[dfam]["launches"]:
             # D pair per iteration: links twice (16 x 72 B FP32, 16 x 36 B FP16), input and output

@@ -215,6 +215,33 @@ def test_block_cg_variant_kernels(gpu, oracle_cls, monkeypatch, flags, variant, 
         assert rel(xs[k], xo) < 1e-7, (k, rel(xs[k], xo))
 
 
+def test_tuner_source_count_classes(gpu, oracle_cls):
+    """The autotuner chooses one shape per class of source counts (1, 2,
+    3-4, 5-8, 9-16), tuned for the class's widest count: after a 5-source
+    block solve on a fresh lattice the 5- and the 8-source D_eo have the
+    same shape, wide enough for 8 sources, and the solve is correct."""
+    import ctypes
+    m = gpu
+    dims = (8, 8, 8, 12)
+    m.set_lattice((4, 4, 4, 4))   # a lattice change drops the shapes chosen earlier
+    orc, fat, lng = _setup(m, oracle_cls, dims)
+    srcs = [m.gen_vector(dims, 900 + k, m.EVEN) for k in range(5)]
+    xs = [np.zeros_like(s) for s in srcs]
+    qic = m.QuarkInvertControl(resid=1e-10, max=2000, nrestart=5, parity=m.EVEN, prec=m.PREC_SINGLE)
+    m.ks_congrad_block_parity(srcs, xs, qic, 0.04)
+    lib = m._lib.load()
+    shapes = []
+    for n in (5, 8):
+        G, nb, block = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        m.check(lib.mks_tuned_shape(m.PREC_SINGLE, n, ctypes.byref(G), ctypes.byref(nb), ctypes.byref(block)),
+                "mks_tuned_shape")
+        shapes.append((G.value, nb.value, block.value))
+    assert shapes[0] == shapes[1] and shapes[0][0] * shapes[0][1] >= 8
+    for k in range(5):
+        _, xo, _ = orc.congrad(fat, lng, srcs[k], np.zeros_like(srcs[k]), 0.04, m.EVEN, 1e-13, 0.0, 2000, 5)
+        assert rel(xs[k], xo) < 1e-7, (k, rel(xs[k], xo))
+
+
 @pytest.mark.parametrize("parity", ["EVEN", "ODD"])
 def test_block_cg_page_locked_host_arrays(gpu, oracle_cls, parity):
     """Page-locked host arrays are read and written in place by the layout
