@@ -22,17 +22,7 @@ __global__ void __launch_bounds__(256) k_site(const Op op, const Fin fin, const 
   double acc[NS];
 #pragma unroll
   for (int k = 0; k < NS; k++) acc[k] = 0.0;
-  // two sites per pass, so that a thread has both sites' loads in flight
-  const int stride = gridDim.x * blockDim.x;
-  int h = blockIdx.x * blockDim.x + threadIdx.x;
-  for (; h + stride < Vh; h += 2 * stride) {
-    double l0[NS], l1[NS];
-    op(h, s, l0);
-    op(h + stride, s, l1);
-#pragma unroll
-    for (int k = 0; k < NSUM; k++) acc[k] += l0[k] + l1[k];
-  }
-  if (h < Vh) {
+  for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < Vh; h += gridDim.x * blockDim.x) {
     double loc[NS];
     op(h, s, loc);
 #pragma unroll
