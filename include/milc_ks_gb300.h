@@ -323,10 +323,12 @@ int mks_bench_dslash(int prec, int nsrc, int parity, int slot, int iters, int fl
                      double *ms);
 
 /* D_eo launch shape chosen by the autotuner for (prec, nsrc): G threads per
- * site, nb sources per thread, block threads per CTA.  The tuner times
- * every candidate on the live links the first time a (prec, nsrc) pair is
- * launched (environment MKS_TUNE=0 keeps a fixed table).  Returns
- * MKS_ERR_STATE when the pair has not been launched yet. */
+ * site, nb sources per thread, block threads per CTA.  The tuner times its
+ * candidates on the live links the first time a precision and a class of
+ * source counts (1, 2, 3-4, 5-8, 9-16) is launched, for the class's widest
+ * count, and every count of the class takes that shape (environment
+ * MKS_TUNE=0 keeps a fixed table).  Returns MKS_ERR_STATE when nsrc has
+ * not been launched yet at this precision. */
 int mks_tuned_shape(int prec, int nsrc, int *G, int *nb, int *block);
 
 /* The same for the launches with the fused CG epilogue (D_eo, axpy and

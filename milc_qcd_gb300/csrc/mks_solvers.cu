@@ -382,11 +382,13 @@ static LinkSet16 links16(const LinkSlot &s) {
 // ------------------------------------------------------------------
 // D_eo launch shapes and their autotuner.
 // A shape is (G threads per site, NB sources per thread, block size).  The
-// first launch for a given (link precision, nsrc) times every candidate
-// with G*NB >= nsrc (and at most 2x padding) on the live links and scratch
-// vectors, keeps the fastest, and reuses it for every epilogue.  MKS_TUNE=0
-// turns tuning off (fixed table); the choices can be read back with
-// mks_tuned_shape().
+// first launch for a given (link precision, class of source counts: 1, 2,
+// 3-4, 5-8, 9-16) times the candidates with G*NB >= the class's widest
+// count (and at most 2x padding) on the live links and scratch vectors,
+// over at most 2^20 sites, keeps the fastest, and reuses it for every count
+// of the class; plain and fused-epilogue launches are tuned apart.
+// MKS_TUNE=0 turns tuning off (fixed table); the choices can be read back
+// with mks_tuned_shape().
 // launch shape: G threads per site, NB sources per thread, block size;
 // tma = 1: the FP32 kernel that stages each tile's links in shared memory
 // (NB = 1, block = T G for a tile of T sites); pipe = 1: the kernel whose
