@@ -327,8 +327,9 @@ int mks_bench_dslash(int prec, int nsrc, int parity, int slot, int iters, int fl
  * candidates on the live links the first time a precision and a class of
  * source counts (1, 2, 3-4, 5-8, 9-16) is launched, for the class's widest
  * count, and every count of the class takes that shape (environment
- * MKS_TUNE=0 keeps a fixed table).  Returns MKS_ERR_STATE when nsrc has
- * not been launched yet at this precision. */
+ * MKS_TUNE=0 keeps a fixed table).  Returns MKS_ERR_STATE when no shape
+ * has been chosen for nsrc yet (a class's widest count has its shape as
+ * soon as any count of the class was launched). */
 int mks_tuned_shape(int prec, int nsrc, int *G, int *nb, int *block);
 
 /* The same for the launches with the fused CG epilogue (D_eo, axpy and
