@@ -12,6 +12,7 @@
 // updated by the last block of each reduction, and kernels return at once
 // while a device flag asks for host attention (restart, reliable update,
 // convergence).  The host only polls that flag every few iterations.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <cstdlib>
@@ -657,16 +658,18 @@ static bool persist_enabled() {
   return v != 0;
 }
 
-// The sloppy multi-shift stops when the lowest shift's residual, recomputed
-// in FP64 by a reliable update, meets the target (the iterated residual
-// alone drifts a little above it, and every shift that misses the target
-// then takes a block-CG refinement from a fresh Krylov space).
-// MKS_MS_TRUE_STOP=0 stops on the iterated residual as the FP64 solve does.
+// The sloppy multi-shift stops on the lowest shift's iterated residual, as
+// the FP64 solve does; the FP64 check of every shift follows.
+// MKS_MS_TRUE_STOP=1 makes it stop only when that shift's residual,
+// recomputed in FP64 by a reliable update, meets the target -- measured on
+// GB300 (11 offsets, 32^3x64, 1e-10) it buys nothing: 0.432 against 0.430 s,
+// the lowest shift then passing the check with one refinement iteration
+// either way.
 static bool ms_true_stop() {
   static int v = -1;
   if (v < 0) {
     const char *e = getenv("MKS_MS_TRUE_STOP");
-    v = e ? atoi(e) : 1;
+    v = e ? atoi(e) : 0;
   }
   return v != 0;
 }
@@ -1184,11 +1187,19 @@ template <class F>
 static int graph_batch(const std::vector<uint64_t> &key, F issue) {
   Context &c = ctx();
   if (!graphs_enabled()) return issue();
+  // least recently used entries are dropped first (the list is kept in
+  // order of use); the solves of a trajectory meet many distinct batches
+  // (active-source sets of the refinements), and a dropped entry costs an
+  // eager run and a new capture when it comes back
   GraphEntry *e = nullptr;
-  for (auto &g : g_graphs)
-    if (g.key == key) { e = &g; break; }
+  for (size_t i = 0; i < g_graphs.size(); i++)
+    if (g_graphs[i].key == key) {
+      if (i + 1 < g_graphs.size()) std::rotate(g_graphs.begin() + i, g_graphs.begin() + i + 1, g_graphs.end());
+      e = &g_graphs.back();
+      break;
+    }
   if (!e) {
-    if (g_graphs.size() >= 32) { free_graph(g_graphs.front()); g_graphs.erase(g_graphs.begin()); }
+    if (g_graphs.size() >= 128) { free_graph(g_graphs.front()); g_graphs.erase(g_graphs.begin()); }
     g_graphs.emplace_back();
     e = &g_graphs.back();
     e->key = key;
@@ -1300,7 +1311,10 @@ static int true_residual(const LinkSlot &sl, int par, int nsrc, const double *ms
 // sources, 32^3x64): the FP64 launches per solve fall from 42 to 20, their
 // time stays the same (the FP64 D is FP64-rate bound per source), and the
 // fewer host polls save 0.7 % of the solve; iteration and update counts are
-// unchanged.
+// unchanged.  Only blocks whose sources share one shift take part: sources
+// of one operator reach their triggers together, while the shifts of a
+// multi-shift refinement do not, and joining them early adds updates (11
+// offsets, 32^3x64: FP64 D 146 ms with the joins, 107 ms without).
 static double ru_join() {
   static double v = -1;
   if (v < 0) {
@@ -1338,6 +1352,8 @@ static int block_cg_shifted(int slot, int par, int nsrc, const double *msq4, con
   MKS_TRY(wsv("cg_state", MAXSRC, &S.st));
   MKS_TRY(wsv("cg_skip", 1, &S.skip));
 
+  bool one_shift = true;            // every source solves the same operator
+  for (int s = 1; s < nsrc; s++) one_shift = one_shift && msq4[s] == msq4[0];
   std::vector<CgState> fin(nsrc);   // final state by original index
   std::vector<int> act, xzero;      // running sources; zero initial guess by block position
   // source norms and initial-guess norms (a zero guess needs no D D x)
@@ -1416,7 +1432,7 @@ static int block_cg_shifted(int slot, int par, int nsrc, const double *msq4, con
       any_host |= hs[k].status == ST_HOST;
       any_run |= hs[k].status == ST_RUN;
     }
-    if (any_host && mixed && !first && ru_join() > 1.0) {
+    if (any_host && mixed && !first && ru_join() > 1.0 && one_shift) {
       // batch the FP64 reliable updates: a running source whose residual is
       // within a factor ru_join() of its own trigger takes its update now,
       // with the sources that asked, in one multi-source FP64 D
