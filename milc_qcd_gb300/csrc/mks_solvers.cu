@@ -674,22 +674,23 @@ static bool ms_true_stop() {
   return v != 0;
 }
 
-// For targets below 1e-7 the sloppy multi-shift keeps the shifts' search
-// directions p_j and solutions x_j in FP64 (residual, D_eo and the lowest
-// shift's D_eo input in FP32).  The update kernel then moves twice the
-// bytes per shift, but fewer shifts miss a tight target after the sloppy
-// phase, so the block-CG refinement that follows shrinks.  Measured on
-// GB300: 11 offsets, 32^3x64, 1e-10: 0.431 against 0.450 s (330 against 353
-// iterations for the slowest shift); the 2+1+1 48^3x96 trajectory, whose
-// molecular-dynamics solves stop at 1e-6: 46.6 s with FP64 storage in every
-// solve against 42.5 s with FP32.  MKS_MS_SHIFT64=1 / 0 forces FP64 / FP32.
-static bool ms_shift64(double resid) {
+// For targets below 1e-7 the sloppy single-field multi-shift keeps the
+// shifts' search directions p_j and solutions x_j in FP64 (residual, D_eo
+// and the lowest shift's D_eo input in FP32).  The update kernel then moves
+// twice the bytes per shift, but fewer shifts miss a tight target after
+// the sloppy phase, so the block-CG refinement that follows shrinks.
+// Measured on GB300 (11 offsets, 32^3x64, 1e-10): 0.392 against 0.425 s
+// (329 against 352 iterations for the slowest shift).  The batched-field
+// solves of the RHMC trajectory keep FP32: the 2+1+1 48^3x96 trajectory
+// took 39.9 s so, 40.4 s with FP64 storage in its 1e-10 solves and 46.6 s
+// with it in every solve.  MKS_MS_SHIFT64=1 / 0 forces FP64 / FP32.
+static bool ms_shift64(double resid, bool batched) {
   static int v = -2;
   if (v == -2) {
     const char *e = getenv("MKS_MS_SHIFT64");
     v = e ? atoi(e) : -1;
   }
-  return v < 0 ? resid < 1e-7 : v != 0;
+  return v < 0 ? (!batched && resid < 1e-7) : v != 0;
 }
 
 static void set_vec(VecF64 &v, float *p, float *) { v.p = (double2 *)p; }
@@ -2613,7 +2614,7 @@ static int multishift_multi_dev_once(int nf, const double *const *src_dev, const
     x64p[f] = x64s[f];
   }
   MsState hs[MSF];
-  if (ms_shift64(arg->resid))
+  if (ms_shift64(arg->resid, true))
     MKS_TRY(multishift_multi_core<double>(sl, par, nf, src64, num_offsets, offs, arg->resid, arg->max * arg->nrestart,
                                           x64p, arg->delta > 0 ? arg->delta : 0.1, hs));
   else
@@ -2695,7 +2696,7 @@ static int multishift_dev_once(const double *src_dev, double *const *psim_dev, c
   // (generic_ks/ks_multicg.c:170-228)
   double2 *x64[MAXSH];
   for (int j = 0; j < nsh; j++) MKS_TRY(wsv("ms_x64_" + std::to_string(j), 3 * c.Vh, &x64[j]));
-  if (ms_shift64(arg->resid))
+  if (ms_shift64(arg->resid, false))
     MKS_TRY((multishift_core<float, double>(sl, par, arg->prec, src64, nsh, offsets, arg->resid, niter, psim, &h,
                                             x64, arg->delta > 0 ? arg->delta : 0.1)));
   else
