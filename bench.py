@@ -792,6 +792,56 @@ def force_workload(args):
     print(json.dumps(line), flush=True)
 
 
+# The 11-offset multi-shift alone (32^3x64, sigma_i = 4m^2 + s_i, s_i
+# log-uniform in [1e-4, 1], to 1e-10; --prec selects the sloppy precision):
+# one warm solve, one timed solve without per-launch events (with its
+# launch counts, for an ncu launch list of exactly that solve), then one
+# with per-launch CUDA events for the kernel families.
+def multishift_workload(args):
+    import torch
+    import milc_qcd_gb300 as m
+    from milc_qcd_gb300 import _lib
+    lib = _lib.load()
+    m.init(0)
+    m.set_lattice(DIMS)
+    m.load_hisq_links(m.apply_phases(DIMS, m.gen_thin_links(DIMS, SEED_LINKS, LINK_A)))
+    prec = {"half": m.PREC_HALF, "single": m.PREC_SINGLE, "double": m.PREC_DOUBLE}[args.prec]
+    sig = 4 * MASS ** 2 + np.logspace(-4, 0, 11)
+    d_b = torch.from_numpy(m.gen_vector(DIMS, SEED_SRC, m.EVEN)).to("cuda")
+    d_p = [torch.zeros_like(d_b) for _ in sig]
+    VP = ctypes.c_void_p * len(sig)
+    arg = _lib.InvertArg(1000, 10, m.EVEN, prec, RESID, 0.0, 0.1)
+    res = (_lib.InvertResult * len(sig))()
+    stream = torch.cuda.ExternalStream(lib.mks_stream())
+
+    def solve():
+        return m.check(lib.mks_ks_multicg_offset_field_dev(d_b.data_ptr(), VP(*[t.data_ptr() for t in d_p]),
+                                                           sig.ctypes.data_as(_lib.DP), len(sig), 0,
+                                                           ctypes.byref(arg), res), "multishift")
+    solve()
+    torch.cuda.synchronize()
+    launches_before = lib.mks_launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    it = solve()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    launches = lib.mks_launch_count() - launches_before
+    lib.mks_timing_reset()
+    lib.mks_timing_enable(1)
+    solve()
+    torch.cuda.synchronize()
+    lib.mks_timing_enable(0)
+    line = {"metric": "11-offset multi-shift CG s per solve (HISQ %s, m=0.01, 1e-10)" % "x".join(map(str, DIMS)),
+            "value": ev0.elapsed_time(ev1) / 1e3, "unit": "s/solve", "n_gpus": 1, "higher_is_better": False,
+            "dtype": {"half": "f16/f32+f64", "single": "f32+f64", "double": "f64"}[args.prec],
+            "data": "synthetic (seeded exp(i 0.3 H) thin links, HISQ smearing on GPU, Gaussian source)",
+            "iters": it, "max_final_rsq": max(r.final_rsq for r in res),
+            "converged": all(r.converged for r in res), "gpu_launches": int(launches),
+            "launches_before_timed": int(launches_before), "kernel_ms": family_times(lib, _lib)}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -809,20 +859,21 @@ def main():
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--md-prec", default="both", choices=["both", "single", "double"],
                     help="force workload: the molecular-dynamics precisions to run")
-    ap.add_argument("--workload", default="cg", choices=["cg", "rhmc", "force"],
+    ap.add_argument("--workload", default="cg", choices=["cg", "rhmc", "force", "multishift"],
                     help="cg: the headline CG benchmark; rhmc: one 2+1+1 HISQ RHMC trajectory; "
-                         "force: HISQ link rebuild + fermion force of one molecular-dynamics step")
+                         "force: HISQ link rebuild + fermion force of one molecular-dynamics step; "
+                         "multishift: the 11-offset multi-shift solve alone")
     args = ap.parse_args()
-    if args.workload in ("rhmc", "force"):
+    if args.dims:
+        global DIMS
+        DIMS = tuple(args.dims)
+    if args.workload in ("rhmc", "force", "multishift"):
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the %s workload has no CPU reference arm"
                               % args.workload}))
             return
-        (rhmc_workload if args.workload == "rhmc" else force_workload)(args)
+        {"rhmc": rhmc_workload, "force": force_workload, "multishift": multishift_workload}[args.workload](args)
         return
-    if args.dims:
-        global DIMS
-        DIMS = tuple(args.dims)
     if args.impl == "reference":
         if args.ref_iters is None:
             args.ref_iters = FP64_ITERS_32C64
