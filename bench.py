@@ -511,11 +511,13 @@ def gpu_arm(args):
     iters = []
     with Clocks() as clk:
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("timed_steps")  # `ncu --nvtx --nvtx-include timed_steps/` takes these launches
         ev0.record(stream)
         for _ in range(args.steps):
             iters.append(solve_dev())
         ev1.record(stream)
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
     launches = lib.mks_launch_count() - launches0
     step_ms = ev0.elapsed_time(ev1) / args.steps
     step_ms = max_over_ranks(step_ms, world, "cuda")
@@ -822,10 +824,12 @@ def multishift_workload(args):
     torch.cuda.synchronize()
     launches_before = lib.mks_launch_count()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("timed_steps")  # `ncu --nvtx --nvtx-include timed_steps/` takes these launches
     ev0.record(stream)
     it = solve()
     ev1.record(stream)
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     launches = lib.mks_launch_count() - launches_before
     lib.mks_timing_reset()
     lib.mks_timing_enable(1)

@@ -719,7 +719,9 @@ static int tune_shape(const LinkT &fat, const LinkT &lng, int nsrc, Shape *best)
     MKS_TRY(wsv("tune_out" + std::to_string(s), n * 4, &out));
     MKS_TRY(wsv("tune_nrm" + std::to_string(s), c.Vh, &nrm));
     k_fill_tune<<<c.sm_count * 4, 256, 0, c.stream>>>(in, n * 4);
+    c.launches++;
     k_fill_tune<<<c.sm_count * 4, 256, 0, c.stream>>>(nrm, c.Vh);
+    c.launches++;
     set_vec(a.in[s], in, nrm);
     set_vec(a.out[s], out, nrm);
     if (EPI == EPI_AXPY) {
@@ -727,7 +729,9 @@ static int tune_shape(const LinkT &fat, const LinkT &lng, int nsrc, Shape *best)
       MKS_TRY(wsv("tune_p" + std::to_string(s), n * 4, &pp));
       MKS_TRY(wsv("tune_r" + std::to_string(s), n * 4, &rr));
       k_fill_tune<<<c.sm_count * 4, 256, 0, c.stream>>>(pp, n * 4);
+      c.launches++;
       k_fill_tune<<<c.sm_count * 4, 256, 0, c.stream>>>(rr, n * 4);
+      c.launches++;
       a.p[s].p = (decltype(a.p[s].p))pp;
       a.r[s].p = (decltype(a.r[s].p))rr;
       a.coef[s] = -0.01;
