@@ -236,6 +236,19 @@ def reference_arm(args):
 
 
 # ---------------------------------------------------------------- extras
+def nvtx_mark(torch, start):
+    """Open (start=True) or close the NVTX range "timed_steps" around the
+    timed launches, so that `ncu --nvtx --nvtx-include timed_steps/` profiles
+    exactly them; a torch without NVTX support skips the marks."""
+    try:
+        if start:
+            torch.cuda.nvtx.range_push("timed_steps")
+        else:
+            torch.cuda.nvtx.range_pop()
+    except Exception:
+        pass
+
+
 def family_times(lib, _lib):
     fam = {}
     for name, k in _lib.KERNEL_FAMILIES.items():
@@ -511,13 +524,13 @@ def gpu_arm(args):
     iters = []
     with Clocks() as clk:
         torch.cuda.synchronize()
-        torch.cuda.nvtx.range_push("timed_steps")  # `ncu --nvtx --nvtx-include timed_steps/` takes these launches
+        nvtx_mark(torch, True)
         ev0.record(stream)
         for _ in range(args.steps):
             iters.append(solve_dev())
         ev1.record(stream)
         torch.cuda.synchronize()
-        torch.cuda.nvtx.range_pop()
+        nvtx_mark(torch, False)
     launches = lib.mks_launch_count() - launches0
     step_ms = ev0.elapsed_time(ev1) / args.steps
     step_ms = max_over_ranks(step_ms, world, "cuda")
@@ -824,12 +837,12 @@ def multishift_workload(args):
     torch.cuda.synchronize()
     launches_before = lib.mks_launch_count()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.nvtx.range_push("timed_steps")  # `ncu --nvtx --nvtx-include timed_steps/` takes these launches
+    nvtx_mark(torch, True)
     ev0.record(stream)
     it = solve()
     ev1.record(stream)
     torch.cuda.synchronize()
-    torch.cuda.nvtx.range_pop()
+    nvtx_mark(torch, False)
     launches = lib.mks_launch_count() - launches_before
     lib.mks_timing_reset()
     lib.mks_timing_enable(1)
