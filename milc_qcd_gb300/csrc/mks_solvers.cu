@@ -2591,6 +2591,16 @@ static int multishift_multi_core(const LinkSlot &sl, int par, int nf, const doub
 // the last multi-shift iteration phase, for the update kernel's byte count
 static long long g_ms_iters = 0, g_ms_shift_updates = 0;
 
+// The block-CG refinement after a sloppy multi-shift runs its inner solve
+// in FP32 when the multi-shift ran in FP16: the multi-source FP16 D_eo is
+// slower than the FP32 one (its half-to-float conversions make it
+// issue-bound), and the refinement solves several shifts at once.
+static mks_invert_arg refine_arg(const mks_invert_arg *arg) {
+  mks_invert_arg a = *arg;
+  if (a.prec == MKS_PREC_HALF) a.prec = MKS_PREC_SINGLE;
+  return a;
+}
+
 static int multishift_multi_dev_once(int nf, const double *const *src_dev, const int *num_offsets,
                                      const double *offsets, double *const *psim_dev, int slot,
                                      const mks_invert_arg *arg, mks_invert_result *res) {
@@ -2640,7 +2650,8 @@ static int multishift_multi_dev_once(int nf, const double *const *src_dev, const
     const int nb = total - b0 < MAXSRC ? total - b0 : MAXSRC;
     CgFields cf;
     memset(&cf, 0, sizeof cf);
-    MKS_TRY(alloc_cg_fields(cf, nb, arg->prec));
+    const mks_invert_arg ra = refine_arg(arg);
+    MKS_TRY(alloc_cg_fields(cf, nb, ra.prec));
     double sig[MAXSRC];
     for (int q = 0; q < nb; q++) {
       const int f = fld[b0 + q], j = shf[b0 + q];
@@ -2648,7 +2659,7 @@ static int multishift_multi_dev_once(int nf, const double *const *src_dev, const
       cf.x[q] = x64s[f][j];
       sig[q] = offs[f][j];
     }
-    MKS_TRY(block_cg_shifted(slot, par, nb, sig, arg, cf, res + b0));
+    MKS_TRY(block_cg_shifted(slot, par, nb, sig, &ra, cf, res + b0));
     for (int q = 0; q < nb; q++) {
       const int f = fld[b0 + q];
       MKS_TRY(vec_soa64_to_aos(cf.x[q], psim_dev[b0 + q], par));
@@ -2713,14 +2724,15 @@ static int multishift_dev_once(const double *src_dev, double *const *psim_dev, c
     int nb = nsh - b0 < MAXSRC ? nsh - b0 : MAXSRC;
     CgFields f;
     memset(&f, 0, sizeof f);
-    MKS_TRY(alloc_cg_fields(f, nb, arg->prec));
+    const mks_invert_arg ra = refine_arg(arg);
+    MKS_TRY(alloc_cg_fields(f, nb, ra.prec));
     for (int s = 0; s < nb; s++) {
       f.src[s] = src64;       // read only in the block CG
       f.x[s] = x64[b0 + s];   // the sloppy solve's FP64 solution is the initial guess
     }
     double sig[MAXSRC];
     for (int s = 0; s < nb; s++) sig[s] = offsets[b0 + s];
-    MKS_TRY(block_cg_shifted(slot, par, nb, sig, arg, f, res + b0));
+    MKS_TRY(block_cg_shifted(slot, par, nb, sig, &ra, f, res + b0));
     for (int s = 0; s < nb; s++) {
       MKS_TRY(vec_soa64_to_aos(f.x[s], psim_dev[b0 + s], par));
       res[b0 + s].final_iters += total_iters;
