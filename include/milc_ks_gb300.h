@@ -182,10 +182,12 @@ int mks_mat_invert_block_uml(int nsrc, const double *const *src, double *const *
  * arrays are read and written in place by the solver's kernels; pageable
  * ones are staged through device copies.
  * arg->prec selects FP64, or FP32/FP16 shifted updates with FP64 reliable
- * updates of the lowest shift (every shift's solution accumulated in FP64),
- * an FP64 true-residual check of every shift, and a mixed-precision
- * refinement of the shifts that miss arg->resid (generic_ks/ks_multicg.c:
- * 170-228). */
+ * updates of the lowest shift (every shift's solution accumulated in FP64;
+ * for arg->resid below 1e-7 the shifts' search directions and solutions
+ * are FP64 vectors), an FP64 true-residual check of every shift, and a
+ * mixed-precision refinement of the shifts that miss arg->resid
+ * (generic_ks/ks_multicg.c:170-228; its inner solve is FP32 when arg->prec
+ * is FP16). */
 int mks_ks_multicg_offset_field(const double *src, double *const *psim,
                                 const double *offsets, int num_offsets, int slot,
                                 const mks_invert_arg *arg, mks_invert_result *res);
