@@ -484,6 +484,13 @@ template <class K> static int resident_blocks(K kernel, int block) {
   return n;
 }
 
+// The variant kernels (software-pipelined, persistent grid, cp.async link
+// buffers) are built for the FP32 plain D_eo only, the launch where they
+// were measured; elsewhere a shape that asks for one runs the direct kernel.
+template <class LinkT, int EPI> constexpr bool has_variants() {
+  return std::is_same<LinkT, LinkF32>::value && EPI == EPI_PLAIN;
+}
+
 template <typename R, class LinkT, class InT, class OutT, int NB, int EPI, int NSUM, class Fin>
 static int launch_dslash_nb(int family, const LinkT &fat, const LinkT &lng,
                             DslashArgs<InT, OutT, typename EpiLoad<R>::type> &a, const Fin &fin, int block,
@@ -492,7 +499,7 @@ static int launch_dslash_nb(int family, const LinkT &fat, const LinkT &lng,
   const size_t sites = family == MKS_K_TUNE && c.Vh > TUNE_SITES ? TUNE_SITES : c.Vh;
   size_t threads = sites * a.groups;
   const int nvb = (int)((threads + block - 1) / block);
-  if constexpr (std::is_same<LinkT, LinkF32>::value) {
+  if constexpr (has_variants<LinkT, EPI>()) {
     if (as == 2 || as == 3) {
       const int grid = nvb;
       a.nvb = 0;
@@ -514,32 +521,43 @@ static int launch_dslash_nb(int family, const LinkT &fat, const LinkT &lng,
       return MKS_OK;
     }
   }
-  auto kp = k_dslash_p<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin>;
   auto k1 = k_dslash1<R, LinkT, InT, OutT, EPI, NSUM, Fin>;
   auto kd = k_dslash<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin>;
-  auto kg = k_dslash_g<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin>;
+  if constexpr (!has_variants<LinkT, EPI>()) {
+    pipe = false;
+    persist = false;
+  }
   if (persist) pipe = false;  // the persistent kernel loads directly
   const bool one = !pipe && !persist && NB == 1 && a.groups == 1 && block == 256;
   int grid = nvb;
   a.nvb = 0;
-  if (persist) {
-    const int cap = resident_blocks(kg, block) * c.sm_count;
-    if (cap < nvb) grid = cap;
-    a.nvb = nvb;
+  if constexpr (has_variants<LinkT, EPI>()) {
+    if (persist) {
+      const int cap = resident_blocks(k_dslash_g<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin>, block) * c.sm_count;
+      if (cap < nvb) grid = cap;
+      a.nvb = nvb;
+    }
   }
   if (NSUM > 0) {
     MKS_TRY(ensure_red(NSUM * a.groups * NB, grid));
     a.red = c.red;
   }
   timing_begin(family);
-  if (persist)
-    kg<<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
-  else if (pipe)
-    kp<<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
-  else if (one)
-    k1<<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
-  else
-    kd<<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
+  if constexpr (has_variants<LinkT, EPI>()) {
+    if (persist)
+      k_dslash_g<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin><<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
+    else if (pipe)
+      k_dslash_p<R, LinkT, InT, OutT, NB, EPI, NSUM, Fin><<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
+    else if (one)
+      k1<<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
+    else
+      kd<<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
+  } else {
+    if (one)
+      k1<<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
+    else
+      kd<<<grid, block, 0, c.stream>>>(fat, lng, a, fin);
+  }
   timing_end(family);
   MKS_CUDA(cudaGetLastError());
   return MKS_OK;
@@ -786,7 +804,8 @@ static int tune_shape(const LinkT &fat, const LinkT &lng, int nsrc, Shape *best)
         const int pipe = cand < 8 ? (cand >> 1) & 1 : 0, persist = cand < 8 ? (cand >> 2) & 1 : 0;
         const int as = cand < 8 ? 0 : 2 + ((cand >> 1) & 1);
         if ((pipe && !pipe_enabled()) || (persist && !persist_enabled()) || (pipe && persist)) continue;
-        if (as && (!std::is_same<LinkT, LinkF32>::value || !async_enabled())) continue;
+        if (as && !async_enabled()) continue;
+        if ((pipe || persist || as) && !has_variants<LinkT, EPI>()) continue;
         Shape sh = {G, NB, block, 0, pipe, persist, as};
         if (memcmp(&sh, &def, sizeof sh) == 0) continue;
         MKS_TRY(try_shape(sh));
@@ -814,8 +833,8 @@ static int tune_shape(const LinkT &fat, const LinkT &lng, int nsrc, Shape *best)
 // "prec:nsrc:G:1:tma" (prec 1, FP32) selects the TMA-staged kernel with G
 // threads per site, where the lattice admits its tiles.  A trailing ":p"
 // selects the software-pipelined kernel, ":g" the persistent grid, ":a2" or
-// ":a3" the cp.async link buffers (FP32).  A leading "d" or "e" limits an
-// entry to the plain D or to the fused-epilogue launches.
+// ":a3" the cp.async link buffers (FP32 plain D only).  A leading "d" or "e"
+// limits an entry to the plain D or to the fused-epilogue launches.
 static bool shape_override(int prec, int nsrc, bool epi, Shape *out) {
   const char *e = getenv("MKS_SHAPE");
   if (!e) return false;
@@ -839,10 +858,13 @@ static bool shape_override(int prec, int nsrc, bool epi, Shape *out) {
         G * NB >= nsrc && G * NB <= MAXSRC && (B == 128 || B == 256)) {
       const size_t f = item.find_first_not_of("0123456789:");
       const std::string flags = f == std::string::npos ? "" : item.substr(f);
-      const int pipe = flags.find('p') != std::string::npos, persist = flags.find('g') != std::string::npos;
+      // the variant kernels exist for the FP32 plain D_eo only
+      const bool var = prec == MKS_PREC_SINGLE && !epi;
+      const int pipe = var && flags.find('p') != std::string::npos;
+      const int persist = var && flags.find('g') != std::string::npos;
       const size_t fa = flags.find('a');
       const int as = (fa != std::string::npos && fa + 1 < flags.size()) ? flags[fa + 1] - '0' : 0;
-      *out = {G, NB, B, 0, pipe, persist, (as == 2 || as == 3) && prec == MKS_PREC_SINGLE ? as : 0};
+      *out = {G, NB, B, 0, pipe, persist, var && (as == 2 || as == 3) ? as : 0};
       return true;
     }
     int T, Rr;
