@@ -357,7 +357,12 @@ static int launch_site(int family, const Op &op, const Fin &fin, const int *skip
   Context &c = ctx();
   int Vh = (int)c.Vh;
   int gx = grid_for(Vh, 256);
-  int cap = c.sm_count * 4;
+  static int per_sm = -1;  // blocks per SM and source (MKS_SITE_BLOCKS, default 4)
+  if (per_sm < 0) {
+    const char *e = getenv("MKS_SITE_BLOCKS");
+    per_sm = e && atoi(e) > 0 ? atoi(e) : 4;
+  }
+  int cap = c.sm_count * per_sm;
   if (gx > cap) gx = cap;
   MKS_TRY(ensure_red(NSUM > 0 ? NSUM * nsrc : 1, gx * nsrc));  // one row per block of the (gx, nsrc) grid
   timing_begin(family);
