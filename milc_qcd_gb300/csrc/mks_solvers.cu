@@ -357,11 +357,19 @@ static int launch_site(int family, const Op &op, const Fin &fin, const int *skip
   Context &c = ctx();
   int Vh = (int)c.Vh;
   int gx = grid_for(Vh, 256);
-  static int per_sm = -1;  // blocks per SM and source (MKS_SITE_BLOCKS, default 4)
-  if (per_sm < 0) {
+  // Blocks per SM and source row: about 16 per SM over all rows, 1 to 4 per
+  // row.  Every block ends with a block reduction and a row of partial sums,
+  // so for many sources fewer, longer blocks win (8 sources on 32^3x64: the
+  // CG's update and dot kernels 111 ms per solve of 8 with 2 per row, 117
+  // with 4, 129 with 8), while the one-row multi-shift update needs the 4
+  // (100 ms against 116 with 2).  MKS_SITE_BLOCKS fixes the count per row.
+  static int forced = -1;
+  if (forced < 0) {
     const char *e = getenv("MKS_SITE_BLOCKS");
-    per_sm = e && atoi(e) > 0 ? atoi(e) : 4;
+    forced = e && atoi(e) > 0 ? atoi(e) : 0;
   }
+  int per_sm = forced ? forced : 16 / (nsrc > 0 ? nsrc : 1);
+  if (!forced) per_sm = per_sm < 1 ? 1 : per_sm > 4 ? 4 : per_sm;
   int cap = c.sm_count * per_sm;
   if (gx > cap) gx = cap;
   MKS_TRY(ensure_red(NSUM > 0 ? NSUM * nsrc : 1, gx * nsrc));  // one row per block of the (gx, nsrc) grid
